@@ -1,0 +1,308 @@
+"""Benchmark of the GB300 stepper on CudaBubble's headline workload.
+
+Workload (one "step" = one accepted step of the hot path): a 128^3 periodic
+grid, seeded ellipsoid phi0 (axes a, b ~ U[1.2, 2], c ~ U[0.5, 1.2], seed 2),
+eps = 1.5 h, M1 = M2 = 1e4, ETD-RK2 with the reference's adaptive dt starting
+at 1e-6 (halve on energy rise, double every 4 accepted steps, cap 1e-3),
+FP32 FFTs / pointwise math with FP64 reductions.  The timed steps are steps
+1..K from phi0 (warm-up runs first on the same workload, then phi0 is
+reloaded).  Every attempt (accepted or rejected) is timed with CUDA events on
+the stepper's stream and L2 is flushed (256 MiB memset) between attempts,
+outside the timed events.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU form (oracle/cstep.c,
+the plain FP64 C port with OpenMP on every host core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_GRID = 128
+EPSSIZE = 150
+SEED = 2
+DT0 = 1e-6
+METRIC = "grid-pts·steps/s vs plain FP64 at rel-E≤1e-6; served p50/p99 latency"
+UNIT = "grid-pt·steps/s"
+FLUSH_BYTES = 256 << 20
+WORKLOAD = ("C2: 128^3 periodic [-pi,pi]^3, seeded ellipsoid phi0 (seed 2), eps=1.5h, M1=M2=1e4, "
+            "ETD-RK2, adaptive dt from 1e-6 (halve on energy rise, x2 every 4 steps, cap 1e-3), steps 1..K from phi0")
+
+
+def phi0():
+    from cudabubble_gb300 import shapes
+    return shapes.seeded_ellipsoid(N_GRID, N_GRID, shapes.eps_rule(EPSSIZE, N_GRID), SEED)
+
+
+def golden_energy(step: int):
+    """The reference's own FP64 cuFFT energy at `step` for this workload, if recorded."""
+    path = os.path.join(ROOT, "tests", "golden", "manifest.json")
+    try:
+        man = json.load(open(path))
+        for s in man["cases"]["c2_etd2_128"]["steps"]:
+            if s["step"] == step:
+                return s["E"]
+    except (OSError, KeyError, ValueError):
+        pass
+    return None
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while active."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_run(nsteps: int, warmup: int, threads: int = 0):
+    """The reference algorithm on the host cores (oracle/cstep.c, FP64, OpenMP)."""
+    from oracle.cbuild import CStep
+    from cudabubble_gb300 import shapes
+    eps = shapes.eps_rule(EPSSIZE, N_GRID)
+    p0 = phi0()
+    cs = CStep(N_GRID, N_GRID, eps, threads=threads)
+    if warmup:
+        cs.set_phi(p0)
+        cs.run("etd2", warmup, DT0, 0.0)
+    cs.set_phi(p0)
+    t0 = time.perf_counter()
+    why = cs.run("etd2", nsteps, DT0, 0.0)
+    dt = time.perf_counter() - t0
+    sc = cs.scalars()
+    cs.close()
+    return dict(seconds=dt, steps=sc["steps"], why=why, threads=cs.threads, E=sc["E"])
+
+
+def cpu_baseline(budget_s: float = 15.0):
+    """Bounded sample: the first S steps of the workload, S sized to ~budget_s."""
+    probe = cpu_reference_run(1, 0)
+    s = max(2, min(64, int(budget_s / max(probe["seconds"], 1e-3))))
+    r = cpu_reference_run(s, 0)
+    return {"value": N_GRID ** 3 * r["steps"] / r["seconds"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+            "sample": f"steps 1..{r['steps']} of the workload on the host (oracle/cstep.c, FP64, OpenMP), "
+                      f"{r['seconds']:.1f} s"}
+
+
+def algorithmic_bytes(n: int, fsize: int, att: int, rej: int):
+    """Bytes each kernel kind must move over `att` attempts with `rej` retries
+    (a retry skips the stage-1 nonlinear pass and reuses the stored N_u).
+    F = one half-spectrum complex field."""
+    F = n * n * (n // 2 + 1) * 2 * fsize
+    return {
+        "xy_nonlin": (2 * att - rej) * 4 * F,          # read P0, P2; write A, B
+        "xy_reduce_s": att * 1 * F,                     # read P0
+        "xy_reduce_full": att * 2 * F,                  # read P0, P2
+        "z_stage": att * 7 * F + (att - rej) * 7 * F + rej * 5 * F,
+        # S2: read A, B, a-hat, N_u; write phi', P0, P2.  S1 fresh: read A, B, phi; write N_u, a-hat, P0, P2
+        # S1 retry: read N_u, phi; write a-hat, P0, P2
+    }, F
+
+
+def run_ours(args, rank: int, world: int):
+    import torch
+    from cudabubble_gb300 import capi
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    p0 = phi0()
+    N = N_GRID ** 3
+    params = capi.default_params(nx=N_GRID, ny=N_GRID, nz=N_GRID, epssize=EPSSIZE, method=capi.CB_ETD2,
+                                 precision=capi.CB_FP32, time_step=DT0, fixed_time_step=0.0, M1=1e4, M2=1e4)
+    st = capi.Stepper(params)
+    # warm-up on the same workload, then reload phi0
+    st.set_phi(p0)
+    st.run(args.warmup)
+    st.set_phi(p0)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        t0 = time.perf_counter()
+        r = st.run_timed(args.steps, FLUSH_BYTES)
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    sc = st.scalars()
+    ms = r["device_ms"]
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    steps = sc["steps"]
+    attempts = r["attempts"]
+    rejects = sc["rejects"]
+    value = world * N * steps / (ms / 1e3)
+    ref_E = golden_energy(steps)
+    rel_E = abs(sc["E"] - ref_E) / abs(ref_E) if ref_E else None
+
+    # per-kernel device time (kernel by kernel, L2 flushed between attempts)
+    st.set_phi(p0)
+    st.run(min(args.steps, 40))  # profile in the steady state after the dt ramp
+    s0 = st.scalars()
+    prof_att = 16
+    prof = st.profile_kernels(prof_att, FLUSH_BYTES)
+    s1 = st.scalars()
+    prej = s1["rejects"] - s0["rejects"]
+    ab, F = algorithmic_bytes(N_GRID, 4, prof_att, prej)
+    kern = {}
+    for k, (kms, cnt) in prof.items():
+        if k in ab and kms > 0:
+            kern[k] = {"ms_total": kms, "launches": cnt, "algorithmic_bytes": ab[k],
+                       "achieved_gbs": ab[k] / (kms / 1e3) / 1e9}
+    total_ms = sum(v[0] for v in prof.values())
+    dom = max(kern, key=lambda k: kern[k]["ms_total"])
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get(dom)
+    d = kern[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(d["achieved_gbs"], 1), "peak": hbm_peak,
+                "unit": "GB/s", "frac": round(d["achieved_gbs"] / hbm_peak, 4), "traffic": traffic,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800",
+                "bytes_per_launch": d["algorithmic_bytes"] / d["launches"],
+                "share_of_step_time": round(d["ms_total"] / total_ms, 3),
+                "per_kernel": {k: {"avg_us": round(1e3 * v["ms_total"] / v["launches"], 2),
+                                   "achieved_gbs": round(v["achieved_gbs"], 1),
+                                   "share": round(v["ms_total"] / total_ms, 3)} for k, v in kern.items()}}
+
+    # end to end through the C ABI with host buffers: set_phi(host) + run(K) + get_phi(host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st.set_phi(p0)
+    rr = st.run(args.steps)
+    out = st.get_phi()
+    sc2 = st.scalars()
+    e2e_s = time.perf_counter() - t0
+    e2e_steps = sc2["steps"]
+    e2e = {"value": world * N * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(p0.nbytes / max(e2e_steps, 1)),
+           "d2h_bytes_per_step": int((out.nbytes + 120) / max(e2e_steps, 1)),
+           "what": "cb_set_phi(host phi0) + cb_run(K) + cb_get_phi(host) + cb_scalars_get, wall clock"}
+    st.close()
+
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
+           "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 (FFT + pointwise), f64 reductions / scalars / energy test", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2", "attempts": attempts,
+                      "rejects": rejects, "l2": "flushed between attempts (256 MiB memset, outside timed events)",
+                      "parallelism": "replicas" if world > 1 else "single GPU", "points": N},
+           "accuracy": {"E_step_K": sc["E"], "E_reference_fp64_cufft": ref_E, "rel_E_error": rel_E},
+           "e2e": e2e, "gpu_launches": attempts * 8, "roofline": roofline,
+           "wall_s_timed_region": wall}
+    clk_sum = clk.summary()
+    res["clocks"] = clk_sum
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        steps = max(1, min(args.steps, 20))
+        r = cpu_reference_run(steps, max(0, min(args.warmup, 3)))
+        v = N_GRID ** 3 * r["steps"] / r["seconds"]
+        res = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": r["steps"],
+               "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2",
+                          "note": "steps capped at 20 per run to bound CPU time"},
+               "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                                "sample": f"steps 1..{r['steps']} of the workload (oracle/cstep.c, FP64, OpenMP on "
+                                          f"{r['threads']} of {cores} host threads)"},
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(res))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

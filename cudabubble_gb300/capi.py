@@ -1,0 +1,217 @@
+"""ctypes binding of ``include/cbstep.h`` (libcbstep.so).
+
+The library is loaded from the package's ``lib/`` directory; importing this
+module never falls back to anything else: if the shared library is missing
+or does not export the declared symbols, the import fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libcbstep.so")
+
+CB_OK, CB_EINVAL, CB_ENOMEM, CB_ECUDA, CB_ENONFINITE, CB_ENOTCONVERGED, CB_ETIMEOUT, CB_EDTUNDERFLOW, \
+    CB_EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
+CB_EULER, CB_ETD2, CB_ETD4 = 0, 1, 2
+CB_FP64, CB_FP32 = 0, 1
+(CB_FIELD_PHI, CB_FIELD_FD, CB_FIELD_LAP, CB_FIELD_F, CB_FIELD_G0, CB_FIELD_NLD, CB_FIELD_DX, CB_FIELD_DY,
+ CB_FIELD_DZ, CB_FIELD_S, CB_FIELD_NLD_HAT, CB_FIELD_RHS) = range(12)
+STATUS_NAMES = {0: "running", 1: "target", 2: "dt_underflow", 3: "small_energy", 4: "nonfinite", 5: "converged",
+                6: "tmax"}
+ERROR_NAMES = {CB_EINVAL: "CB_EINVAL", CB_ENOMEM: "CB_ENOMEM", CB_ECUDA: "CB_ECUDA", CB_ENONFINITE: "CB_ENONFINITE",
+               CB_ENOTCONVERGED: "CB_ENOTCONVERGED", CB_ETIMEOUT: "CB_ETIMEOUT",
+               CB_EDTUNDERFLOW: "CB_EDTUNDERFLOW", CB_EUNSUPPORTED: "CB_EUNSUPPORTED"}
+
+
+class cb_params(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("lenx", C.c_double), ("epssize", C.c_int),
+                ("eps", C.c_double), ("eta", C.c_double), ("ga", C.c_double), ("alpha", C.c_double),
+                ("beta", C.c_double), ("M1", C.c_double), ("M2", C.c_double), ("time_step", C.c_double),
+                ("fixed_time_step", C.c_double), ("tmax", C.c_double), ("method", C.c_int),
+                ("precision", C.c_int), ("grow_every", C.c_int), ("grow_factor", C.c_double),
+                ("dt_cap", C.c_double), ("cap_probe", C.c_double), ("etd4_textbook", C.c_int),
+                ("accurate_coefficients", C.c_int)]
+
+
+class cb_scalars(C.Structure):
+    _fields_ = [("V", C.c_double), ("S", C.c_double), ("E_el", C.c_double), ("E", C.c_double),
+                ("lamb1", C.c_double), ("lamb2", C.c_double), ("alpha", C.c_double), ("beta", C.c_double),
+                ("dt", C.c_double), ("t", C.c_double), ("lserror", C.c_double), ("steps", C.c_int),
+                ("attempts", C.c_int), ("rejects", C.c_int), ("status", C.c_int)]
+
+
+class cb_run_stats(C.Structure):
+    _fields_ = [("steps", C.c_int), ("attempts", C.c_int), ("status", C.c_int), ("graph_launches", C.c_int),
+                ("device_ms", C.c_double)]
+
+
+# every symbol include/cbstep.h declares, with its ctypes signature
+_P = C.POINTER
+SIGNATURES = {
+    "cb_params_default": (None, [_P(cb_params)]),
+    "cb_params_from_ini_line": (C.c_int, [C.c_char_p, _P(cb_params)]),
+    "cb_params_eps": (C.c_double, [_P(cb_params)]),
+    "cb_instance_bytes": (C.c_longlong, [_P(cb_params)]),
+    "cb_supported": (C.c_int, [_P(cb_params)]),
+    "cb_create": (C.c_int, [_P(cb_params), _P(C.c_void_p)]),
+    "cb_destroy": (C.c_int, [C.c_void_p]),
+    "cb_set_phi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "cb_get_phi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "cb_scalars_get": (C.c_int, [C.c_void_p, _P(cb_scalars)]),
+    "cb_getstaticenergy": (C.c_double, [C.c_void_p]),
+    "cb_ETD2RK": (C.c_int, [C.c_void_p]),
+    "cb_ETD4RK": (C.c_int, [C.c_void_p]),
+    "cb_euler_step": (C.c_int, [C.c_void_p]),
+    "cb_run": (C.c_int, [C.c_void_p, C.c_int, _P(cb_run_stats)]),
+    "cb_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "cb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
+    "cb_synchronize": (C.c_int, [C.c_void_p]),
+    "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
+    "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
+    "cb_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
+    "cb_last_error": (C.c_char_p, []),
+    "cb_version": (C.c_char_p, []),
+}
+
+
+class CBError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    if not os.path.exists(path):
+        raise ImportError(f"libcbstep.so not built at {path}; run cudabubble_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)  # AttributeError when a declared symbol is missing
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load()
+    return _lib
+
+
+def check(rc: int):
+    if rc != CB_OK:
+        raise CBError(rc, lib().cb_last_error().decode())
+    return rc
+
+
+def default_params(**kw) -> cb_params:
+    p = cb_params()
+    lib().cb_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def params_from_ini(line: str) -> cb_params:
+    p = cb_params()
+    check(lib().cb_params_from_ini_line(line.encode(), C.byref(p)))
+    return p
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Stepper:
+    """One stepper instance (``cb_handle``)."""
+
+    def __init__(self, params: cb_params):
+        self.params = params
+        h = C.c_void_p()
+        check(lib().cb_create(C.byref(params), C.byref(h)))
+        self.h = h
+        self.shape = (params.nz, params.nx, params.nx)
+        self.cshape = (params.nz, params.nx, params.nx // 2 + 1)
+
+    def close(self):
+        if self.h:
+            lib().cb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_phi(self, phi: np.ndarray):
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        assert a.shape == self.shape, (a.shape, self.shape)
+        check(lib().cb_set_phi(self.h, _dptr(a), 0))
+
+    def get_phi(self) -> np.ndarray:
+        out = np.empty(self.shape, np.float64)
+        check(lib().cb_get_phi(self.h, _dptr(out), 0))
+        return out
+
+    def scalars(self) -> dict:
+        s = cb_scalars()
+        check(lib().cb_scalars_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in cb_scalars._fields_}
+
+    def field(self, which: int) -> np.ndarray:
+        if which in (CB_FIELD_FD, CB_FIELD_NLD_HAT):
+            out = np.empty(self.cshape, np.complex128)
+        else:
+            out = np.empty(self.shape, np.float64)
+        check(lib().cb_field(self.h, which, _dptr(out), 0))
+        return out
+
+    def ETD2RK(self):
+        check(lib().cb_ETD2RK(self.h))
+
+    def ETD4RK(self):
+        check(lib().cb_ETD4RK(self.h))
+
+    def euler_step(self):
+        check(lib().cb_euler_step(self.h))
+
+    def set_dt(self, dt: float):
+        check(lib().cb_set_dt(self.h, dt))
+
+    def run_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
+        ms = C.c_double(0.0)
+        att = C.c_int(0)
+        rc = lib().cb_run_timed(self.h, nsteps, flush_bytes, C.byref(ms), C.byref(att))
+        if rc not in (CB_OK, CB_ENONFINITE, CB_EDTUNDERFLOW):
+            check(rc)
+        return {"device_ms": ms.value, "attempts": att.value, "rc": rc}
+
+    KERNEL_KINDS = ("xy_nonlin", "xy_reduce_s", "xy_reduce_full", "z_stage", "decide_coef")
+
+    def profile_kernels(self, nattempts: int, flush_bytes: int = 0) -> dict:
+        ms = (C.c_double * 5)()
+        cnt = (C.c_int * 5)()
+        check(lib().cb_profile_kernels(self.h, nattempts, flush_bytes, ms, cnt))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.KERNEL_KINDS)}
+
+    def nbytes(self) -> int:
+        return int(lib().cb_handle_bytes(self.h))
+
+    def run(self, nsteps: int) -> dict:
+        st = cb_run_stats()
+        rc = lib().cb_run(self.h, nsteps, C.byref(st))
+        res = {k: getattr(st, k) for k, _ in cb_run_stats._fields_}
+        res["rc"] = rc
+        if rc not in (CB_OK, CB_ENONFINITE, CB_EDTUNDERFLOW):
+            check(rc)
+        return res

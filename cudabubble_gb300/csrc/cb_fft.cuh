@@ -1,0 +1,300 @@
+// Device primitives for the GB300 spectral stepper: complex helpers,
+// register-resident DFT codelets, and in-place shared-memory line FFTs.
+//
+// Line FFTs of length L = R1*R2 are split into two register phases (a
+// "four-step" factorisation).  Two in-place variants exist:
+//   * fft_lines_NT: natural-order input  -> "transposed"-order output;
+//   * fft_lines_TN: "transposed"-order input -> natural-order output.
+// Element k of a transposed line lives at position tpos<L>(k) =
+// (k / R1) + R2 * (k % R1).  Every phase reads and writes the same slots, so
+// threads never race on a permutation and only a __syncthreads() separates
+// the two phases.  A transform and its inverse are always paired NT then TN,
+// so no explicit reordering pass is ever needed.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cb {
+
+// ---------------------------------------------------------------- complex
+template <class T> struct CT;
+template <> struct CT<float> { using type = float2; };
+template <> struct CT<double> { using type = double2; };
+template <class T> using cplx = typename CT<T>::type;
+
+template <class C> __device__ __forceinline__ C cmk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
+template <class C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
+template <class C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+template <class C> __device__ __forceinline__ C cmul(C a, C b) { return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+template <class C> __device__ __forceinline__ C cmulc(C a, C b) { return cmk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }  // a*conj(b)
+template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, -a.y); }
+template <class C, class T> __device__ __forceinline__ C cscale(C a, T s) { return cmk<C>(a.x * s, a.y * s); }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, class C> __device__ __forceinline__ C cmul_mi(C a) { return INV ? cmk<C>(-a.y, a.x) : cmk<C>(a.y, -a.x); }
+
+// ------------------------------------------------- compile-time twiddles
+// cos(pi * a / b) for b in {6, 8}: the only angles the radix <= 16 codelets
+// need.  Values are the exact algebraic constants cos(pi/8), sqrt(2)/2,
+// sin(pi/8), sqrt(3)/2 written to double precision.
+__host__ __device__ constexpr double cospi_frac(int a, int b) {
+    // reduce to [0, 2b)
+    return (b == 8)
+        ? ((a % 16 + 16) % 16 == 0 ? 1.0 : (a % 16 + 16) % 16 == 1 ? 0.92387953251128675613
+         : (a % 16 + 16) % 16 == 2 ? 0.70710678118654752440 : (a % 16 + 16) % 16 == 3 ? 0.38268343236508977173
+         : (a % 16 + 16) % 16 == 4 ? 0.0 : (a % 16 + 16) % 16 == 5 ? -0.38268343236508977173
+         : (a % 16 + 16) % 16 == 6 ? -0.70710678118654752440 : (a % 16 + 16) % 16 == 7 ? -0.92387953251128675613
+         : (a % 16 + 16) % 16 == 8 ? -1.0 : (a % 16 + 16) % 16 == 9 ? -0.92387953251128675613
+         : (a % 16 + 16) % 16 == 10 ? -0.70710678118654752440 : (a % 16 + 16) % 16 == 11 ? -0.38268343236508977173
+         : (a % 16 + 16) % 16 == 12 ? 0.0 : (a % 16 + 16) % 16 == 13 ? 0.38268343236508977173
+         : (a % 16 + 16) % 16 == 14 ? 0.70710678118654752440 : 0.92387953251128675613)
+        : ((a % 12 + 12) % 12 == 0 ? 1.0 : (a % 12 + 12) % 12 == 1 ? 0.86602540378443864676
+         : (a % 12 + 12) % 12 == 2 ? 0.5 : (a % 12 + 12) % 12 == 3 ? 0.0
+         : (a % 12 + 12) % 12 == 4 ? -0.5 : (a % 12 + 12) % 12 == 5 ? -0.86602540378443864676
+         : (a % 12 + 12) % 12 == 6 ? -1.0 : (a % 12 + 12) % 12 == 7 ? -0.86602540378443864676
+         : (a % 12 + 12) % 12 == 8 ? -0.5 : (a % 12 + 12) % 12 == 9 ? 0.0
+         : (a % 12 + 12) % 12 == 10 ? 0.5 : 0.86602540378443864676);
+}
+// cos / sin of 2*pi*m/R for R in {2, 3, 4, 6, 8, 12, 16}
+__host__ __device__ constexpr double cos2pi(int m, int R) {
+    return (R == 16) ? cospi_frac(m, 8) : (R == 8) ? cospi_frac(2 * m, 8) : (R == 4) ? cospi_frac(4 * m, 8)
+         : (R == 2) ? cospi_frac(8 * m, 8) : (R == 12) ? cospi_frac(m, 6) : (R == 6) ? cospi_frac(2 * m, 6)
+         : cospi_frac(4 * m, 6);
+}
+__host__ __device__ constexpr double sin2pi(int m, int R) {  // sin(x) = cos(x - pi/2)
+    return (R == 16) ? cospi_frac(m - 4, 8) : (R == 8) ? cospi_frac(2 * m - 4, 8) : (R == 4) ? cospi_frac(4 * m - 4, 8)
+         : (R == 2) ? cospi_frac(8 * m - 4, 8) : (R == 12) ? cospi_frac(m - 3, 6) : (R == 6) ? cospi_frac(2 * m - 3, 6)
+         : cospi_frac(4 * m - 3, 6);
+}
+// W_R^m = exp(-+ 2 pi i m / R): forward uses the minus sign
+template <class C, bool INV> __device__ __forceinline__ C wconst(int m, int R) {
+    using T = decltype(C::x);
+    return cmk<C>((T)cos2pi(m, R), INV ? (T)sin2pi(m, R) : -(T)sin2pi(m, R));
+}
+
+// ------------------------------------------------------------ codelets
+// In-register DFT of size R, natural order in and out:
+// A[k] = sum_j a[j] * W_R^{jk}, W_R = exp(-2 pi i / R) (forward) or its conjugate.
+template <int R, bool INV, class C> struct DFT;
+
+template <bool INV, class C> struct DFT<1, INV, C> {
+    static __device__ __forceinline__ void run(C*) {}
+};
+template <bool INV, class C> struct DFT<2, INV, C> {
+    static __device__ __forceinline__ void run(C* a) {
+        C t = a[0];
+        a[0] = cadd(t, a[1]);
+        a[1] = csub(t, a[1]);
+    }
+};
+template <bool INV, class C> struct DFT<3, INV, C> {
+    static __device__ __forceinline__ void run(C* a) {
+        using T = decltype(C::x);
+        const T h = (T)0.86602540378443864676;
+        C s = cadd(a[1], a[2]);
+        C d = csub(a[1], a[2]);
+        C m = cmk<C>(a[0].x - (T)0.5 * s.x, a[0].y - (T)0.5 * s.y);
+        C r = cmul_mi<INV>(d);  // -i d (fwd) / +i d (inv)
+        a[0] = cadd(a[0], s);
+        a[1] = cmk<C>(m.x + h * r.x, m.y + h * r.y);
+        a[2] = cmk<C>(m.x - h * r.x, m.y - h * r.y);
+    }
+};
+template <bool INV, class C> struct DFT<4, INV, C> {
+    static __device__ __forceinline__ void run(C* a) {
+        C s0 = cadd(a[0], a[2]), d0 = csub(a[0], a[2]);
+        C s1 = cadd(a[1], a[3]), d1 = cmul_mi<INV>(csub(a[1], a[3]));
+        a[0] = cadd(s0, s1);
+        a[2] = csub(s0, s1);
+        a[1] = cadd(d0, d1);
+        a[3] = csub(d0, d1);
+    }
+};
+template <int R> struct Split {  // R = P * Q with P in {4, 3, 2}
+    static constexpr int P = (R % 4 == 0 && R != 4) ? 4 : (R % 3 == 0 && R != 3) ? 3 : 2;
+    static constexpr int Q = R / P;
+};
+// composite codelet: four-step in registers with compile-time twiddles
+template <int R, bool INV, class C> struct DFT {
+    static __device__ __forceinline__ void run(C* a) {
+        constexpr int P = Split<R>::P, Q = Split<R>::Q;  // input j = j2 + Q*j1, output k = k1 + P*k2
+        C y[R];
+#pragma unroll
+        for (int j2 = 0; j2 < Q; ++j2) {
+            C t[P];
+#pragma unroll
+            for (int j1 = 0; j1 < P; ++j1) t[j1] = a[j2 + Q * j1];
+            DFT<P, INV, C>::run(t);
+#pragma unroll
+            for (int k1 = 0; k1 < P; ++k1)
+                y[j2 + Q * k1] = (j2 * k1 == 0) ? t[k1] : cmul(t[k1], wconst<C, INV>((j2 * k1) % R, R));
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            C t[Q];
+#pragma unroll
+            for (int j2 = 0; j2 < Q; ++j2) t[j2] = y[j2 + Q * k1];
+            DFT<Q, INV, C>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < Q; ++k2) a[k1 + P * k2] = t[k2];
+        }
+    }
+};
+
+// ------------------------------------------------- line FFT factorisation
+template <int L> struct Plan;  // L = R1 * R2, both <= 16
+template <> struct Plan<8> { static constexpr int R1 = 8, R2 = 1; };
+template <> struct Plan<12> { static constexpr int R1 = 12, R2 = 1; };
+template <> struct Plan<16> { static constexpr int R1 = 16, R2 = 1; };
+template <> struct Plan<24> { static constexpr int R1 = 8, R2 = 3; };
+template <> struct Plan<32> { static constexpr int R1 = 8, R2 = 4; };
+template <> struct Plan<48> { static constexpr int R1 = 8, R2 = 6; };
+template <> struct Plan<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct Plan<96> { static constexpr int R1 = 16, R2 = 6; };
+template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
+template <> struct Plan<192> { static constexpr int R1 = 16, R2 = 12; };
+template <> struct Plan<256> { static constexpr int R1 = 16, R2 = 16; };
+
+// slot of output element k of an NT transform (identity when R2 == 1)
+template <int L> __host__ __device__ __forceinline__ int tpos(int k) {
+    constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
+    return (R2 == 1) ? k : (k / R1) + R2 * (k % R1);
+}
+// element index held by slot p of a transposed line (inverse of tpos)
+template <int L> __host__ __device__ __forceinline__ int tidx(int p) {
+    constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
+    return (R2 == 1) ? p : (p / R2) + R1 * (p % R2);
+}
+
+// twiddle from a table of W_L^m (forward sign), conjugated for the inverse
+template <bool INV, class C> __device__ __forceinline__ C tw_get(const C* tw, int m) {
+    C w = tw[m];
+    return INV ? cconj(w) : w;
+}
+
+// Line offsets: line l starts at buf + off(l).
+struct LinearLines {
+    int ls;
+    __device__ __forceinline__ int operator()(int l) const { return l * ls; }
+};
+// two fields side by side in one padded plane: lines [0, n1) are rows of
+// field 0, lines [n1, 2 n1) rows of field 1 (which starts `second` slots in)
+struct PairRows {
+    int n1, pitch, second;
+    __device__ __forceinline__ int operator()(int l) const {
+        return (l < n1) ? l * pitch : (l - n1) * pitch + second;
+    }
+};
+
+// NT: natural in -> transposed out.  Lines l in [0, nlines) at buf + off(l),
+// element stride es.  All NTHR threads of the block call it; caller syncs after.
+template <int L, bool INV, int NTHR, class C, class OFF>
+__device__ __forceinline__ void fft_lines_NT(C* buf, int nlines, OFF off, int es, const C* tw) {
+    constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
+    const int tid = threadIdx.x;
+    if constexpr (R2 == 1) {
+        for (int l = tid; l < nlines; l += NTHR) {
+            C a[R1];
+            C* p = buf + off(l);
+#pragma unroll
+            for (int j = 0; j < R1; ++j) a[j] = p[j * es];
+            DFT<R1, INV, C>::run(a);
+#pragma unroll
+            for (int j = 0; j < R1; ++j) p[j * es] = a[j];
+        }
+    } else {
+    // phase A: for each (line, j2) DFT_R1 over j1 of x[j2 + R2 j1], twiddle W_L^{j2 k1}
+    for (int it = tid; it < nlines * R2; it += NTHR) {
+        const int l = it % nlines, j2 = it / nlines;
+        C* p = buf + off(l) + j2 * es;
+        C a[R1];
+#pragma unroll
+        for (int j1 = 0; j1 < R1; ++j1) a[j1] = p[j1 * R2 * es];
+        DFT<R1, INV, C>::run(a);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) {
+            C v = (k1 == 0) ? a[k1] : cmul(a[k1], tw_get<INV>(tw, (j2 * k1) % L));
+            p[k1 * R2 * es] = v;
+        }
+    }
+    __syncthreads();
+    // phase B: for each (line, k1) DFT_R2 over j2 of the contiguous block at R2*k1
+    for (int it = tid; it < nlines * R1; it += NTHR) {
+        const int l = it % nlines, k1 = it / nlines;
+        C* p = buf + off(l) + (R2 * k1) * es;
+        C a[R2];
+#pragma unroll
+        for (int j2 = 0; j2 < R2; ++j2) a[j2] = p[j2 * es];
+        DFT<R2, INV, C>::run(a);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) p[k2 * es] = a[k2];
+    }
+    }
+}
+
+// TN: transposed in -> natural out (input element j = j1 + R1 j2 sits at
+// slot j2 + R2 j1, exactly where an NT transform leaves element j).
+template <int L, bool INV, int NTHR, class C, class OFF>
+__device__ __forceinline__ void fft_lines_TN(C* buf, int nlines, OFF off, int es, const C* tw) {
+    constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
+    const int tid = threadIdx.x;
+    if constexpr (R2 == 1) {
+        fft_lines_NT<L, INV, NTHR, C, OFF>(buf, nlines, off, es, tw);
+    } else {
+    // phase A: for each (line, j1) DFT_R2 over j2 (contiguous block at R2*j1), twiddle W_L^{j1 k2}
+    for (int it = tid; it < nlines * R1; it += NTHR) {
+        const int l = it % nlines, j1 = it / nlines;
+        C* p = buf + off(l) + (R2 * j1) * es;
+        C a[R2];
+#pragma unroll
+        for (int j2 = 0; j2 < R2; ++j2) a[j2] = p[j2 * es];
+        DFT<R2, INV, C>::run(a);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+            C v = (k2 == 0) ? a[k2] : cmul(a[k2], tw_get<INV>(tw, (j1 * k2) % L));
+            p[k2 * es] = v;
+        }
+    }
+    __syncthreads();
+    // phase B: for each (line, k2) DFT_R1 over j1 at stride R2 -> X[k2 + R2 k1] at the same slots
+    for (int it = tid; it < nlines * R2; it += NTHR) {
+        const int l = it % nlines, k2 = it / nlines;
+        C* p = buf + off(l) + k2 * es;
+        C a[R1];
+#pragma unroll
+        for (int j1 = 0; j1 < R1; ++j1) a[j1] = p[j1 * R2 * es];
+        DFT<R1, INV, C>::run(a);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) p[k1 * R2 * es] = a[k1];
+    }
+    }
+}
+
+// ------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// Block-wide sum of NV doubles; the result is valid in thread 0.  `red` must
+// hold 32*NV doubles of shared memory.
+template <int NV>
+__device__ __forceinline__ void block_sum(double* v, double* red) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[i * 32 + w] = v[i];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = (lane < nw) ? red[i * 32 + lane] : 0.0;
+            v[i] = warp_sum(s);
+        }
+    }
+}
+
+}  // namespace cb

@@ -1,0 +1,101 @@
+// Host/device shared definitions of one stepper instance (one vesicle).
+//
+// HBM layout of an instance (T = float for the precision form, double for
+// the plain FP64 form; C = complex T):
+//   spectra      C[nz][ny][nx/2+1]  phi-hat (x2: state / candidate), a-hat,
+//                                   N_u, N_a, N_b (nonlinear spectra)
+//   partials     C[nz][ny][nx/2+1]  z-inverted (real z, spectral y/x) fields
+//                                   P0 = IFFT_z(u-hat), P2 = IFFT_z(-kz^2 u-hat)
+//                                   for three states (state / candidate / work)
+//                                   and the nonlinear partials A, B
+//   coef         T[(kmax+1)*8]      ETD coefficients indexed by the integer |k|^2
+//   ctrl         Ctrl               FP64 scalars, dt, accept/reject state
+// The forward 3-D transform is normalised by 1/N, as in the reference
+// (Calc.cu:88-96); the inverse is not.
+#pragma once
+#include <stdint.h>
+
+namespace cb {
+
+enum Method { M_EULER = 0, M_ETD2 = 1, M_ETD4 = 2 };
+
+// which Scal / partial set a kernel works on
+enum Role { R_STATE = 0, R_CAND = 1, R_WORK = 2, R_NROLE = 3 };
+
+// FP64 reductions of one state.  Means are over the N grid points.
+struct Scal {
+    double sum_u;   // sum of u (real space)
+    double sum_s2;  // sum of (u^2-1)^2
+    double sum_f2;  // sum of f^2, f = -eps lap u + (u^2-1) u / eps
+    double grad2;   // mean |grad u|^2 via Parseval over the half spectrum
+    double lsq;     // mean R^2 of the Euler right-hand side (LSerror) via Parseval
+    double V, S, E_el, E;
+    double pad[3];
+};
+
+struct Ctrl {
+    double dt;        // time step of the next attempt
+    double dt_tab;    // time step the coefficient table was built for (0: none)
+    double t;         // accepted time
+    double alpha, beta, alpha0, beta0;
+    double E_state;   // energy of the accepted state
+    double E_init;    // energy at the start of the run (fixed-dt exit test, belastic.cpp:617,727)
+    double E_last_attempt;
+    int steps;        // accepted steps
+    int attempts;
+    int rejects;
+    int fresh;        // 1: stage-1 nonlinear term must be recomputed
+    int done;         // 1: instance finished (kernels skip it)
+    int status;       // CB_OK or an error / exit reason
+    int target;       // accepted steps to take before done
+    int spec_state;   // index (0/1) of the state phi-hat buffer
+    int part_state;   // index (0/1) of the state partial set
+    int corr_phase;   // alpha/beta correction sub-step (fixed dt, M != 0)
+    int nonfinite;
+    int pad0;
+    unsigned cnt_xy[R_NROLE];  // last-block-done counters per role
+    unsigned cnt_z[R_NROLE];
+    Scal sc[R_NROLE];
+};
+
+struct Params {
+    int nx, ny, nz, nc;
+    long long N;
+    int method;         // Method
+    int adaptive;       // 1: energy accept/reject with dt schedule
+    int corr;           // 1: alpha/beta correction double step (fixed dt, M != 0)
+    int etd4_ref;       // 1: reference combine (N_a in the first slot, belastic.cpp:550)
+    int kmax;           // largest folded |k|^2 index
+    int grow_every;     // grow dt every this many accepted steps
+    double eps, eta, ga, M1, M2;
+    double cx;          // (2 pi / L)^2
+    double L3;          // box volume
+    double invN;
+    double grow_factor, dt_cap, cap_probe, dt_min;
+    double tmax;        // Euler loop time limit (belastic.cpp:407)
+};
+
+// exit reasons kept in Ctrl::status (mirrors the public CB_* codes)
+enum { ST_RUNNING = 0, ST_TARGET = 1, ST_DT_UNDERFLOW = 2, ST_SMALL_ENERGY = 3, ST_NONFINITE = 4, ST_CONVERGED = 5,
+       ST_TMAX = 6 };
+
+template <class T> struct InstT {
+    void* spec[2];  // phi-hat state / candidate (swap via ctrl->spec_state)
+    void* ahat;
+    void* Nu;
+    void* Na;
+    void* Nb;
+    void* P[3][2];  // partial sets: [0],[1] state/candidate (swap via ctrl->part_state), [2] work
+    void* A;
+    void* B;
+    T* coef;
+    Ctrl* ctrl;
+    double* part_xy;  // [nz][4] per-plane partial sums
+    double* part_z;   // [ntiles][2] per-tile partial sums
+    const void* twx;  // W_{nx/2}^m (nx/2 entries) then W_nx^m (nx entries)
+    const void* twy;  // W_ny^m
+    const void* twz;  // W_nz^m
+    Params p;
+};
+
+}  // namespace cb

@@ -1,0 +1,43 @@
+// Launch arguments of the stepper kernels (host/device shared).
+#pragma once
+
+namespace cb {
+
+enum XYMode { XY_REDUCE_FULL = 0, XY_REDUCE_S = 1, XY_NONLIN = 2, XY_INV_PLAIN = 3, XY_FWD_PLAIN = 4 };
+
+struct XYArgs {
+    int mode;
+    int role;           // partial set and Scal record the pass reads / writes
+    int skip_if_stale;  // XY_NONLIN on the state: skip when the stored N_u is reused
+    int pad;
+    const void* cin;    // XY_INV_PLAIN: partial C[nz][ny][nc]
+    double* rout;       // XY_INV_PLAIN: real double[nz][ny][nx]
+    const double* rin;  // XY_FWD_PLAIN: real double[nz][ny][nx]
+    void* cout;         // XY_FWD_PLAIN: partial C[nz][ny][nc]
+};
+
+enum ZMode {
+    Z_ETD2_S1 = 0,  // N_u (fresh) ; a-hat = e phi-hat + c1 N_u                     (Calc.cu:446-457)
+    Z_ETD2_S2,      // phi-hat' = a-hat + c2 (N_a - N_u)                           (Calc.cu:466-479)
+    Z_ETD4_S1,      // N_u ; a-hat = e_h phi-hat + c_h N_u                          (Calc.cu:488-499)
+    Z_ETD4_S2,      // N_a ; b-hat = e_h phi-hat + c_h N_a                          (Calc.cu:509-520)
+    Z_ETD4_S3,      // N_b ; c-hat = e_h a-hat + c_h (2 N_b - N_u)                  (Calc.cu:529-540)
+    Z_ETD4_S4,      // phi-hat' = e2 phi-hat + f1 N1 + f2 (N1 + N_b) + f3 N_c      (Calc.cu:549-569)
+    Z_EULER,        // phi-hat' = phi-hat - dt ga R-hat                             (Calc.cu:393-402)
+    Z_INV_STATE,    // partials + Parseval of an existing spectrum (set-up / restore)
+    Z_FWD_PLAIN,    // partial -> spectrum (x 1/N)
+    Z_INV_PLAIN,    // spectrum (x multiplier) -> partial P0
+};
+
+enum SpecMul { SM_NONE = 0, SM_LAP = 1, SM_DX = 2, SM_DY = 3, SM_DZ = 4 };
+
+struct ZArgs {
+    int mode;
+    int role;      // partial set / Scal record written (stage modes), spectrum read (Z_INV_STATE)
+    int mul;       // SpecMul for Z_INV_PLAIN
+    int pad;
+    const void* cin;
+    void* cout;
+};
+
+}  // namespace cb

@@ -1,0 +1,25 @@
+// Typed kernel launchers; one explicit instantiation per precision lives in
+// kernels_f32.cu / kernels_f64.cu so the two compile in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "cb_inst.h"
+#include "cb_kargs.h"
+
+namespace cb {
+
+template <class T> struct Launch {
+    static bool xy_supported(int nx);
+    static bool z_supported(int nz);
+    static int z_tile();
+    static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s);
+    static cudaError_t z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s);
+    static cudaError_t decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s);
+    static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s);
+    static cudaError_t to_double(const void* in, double* out, size_t n, cudaStream_t s);
+};
+
+cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,
+                             const double* d, double eps, double x0, double x1, double x2, cudaStream_t s);
+
+}  // namespace cb

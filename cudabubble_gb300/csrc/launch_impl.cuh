@@ -1,0 +1,107 @@
+// Size dispatch for the kernel templates (included by kernels_f32.cu and
+// kernels_f64.cu with CB_REAL set to float or double).
+#pragma once
+#include "launch.h"
+#include "misc_kernels.cuh"
+#include "xy_kernel.cuh"
+#include "z_kernel.cuh"
+
+namespace cb {
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+template <class T, int NX> struct XYCfg {
+    static constexpr int NT = NX <= 32 ? 128 : (NX <= 64 ? 256 : 512);
+    static constexpr bool ok = xy_smem_bytes<T, NX>(2) <= kMaxSmem;
+};
+
+template <class T, int NX>
+static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    if constexpr (!XYCfg<T, NX>::ok) {
+        return cudaErrorInvalidValue;
+    } else {
+        constexpr int NT = XYCfg<T, NX>::NT;
+        static bool attr = false;
+        if (!attr) {
+            cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)xy_smem_bytes<T, NX>(2));
+            if (e != cudaSuccess) return e;
+            attr = true;
+        }
+        const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
+        xy_kernel<T, NX, NT><<<dim3(nzmax, ninst), NT, xy_smem_bytes<T, NX>(nf), s>>>(d, a);
+        return cudaGetLastError();
+    }
+}
+
+template <class T> constexpr int ztile() { return sizeof(T) == 4 ? 16 : 8; }
+
+template <class T, int NZ>
+static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
+    constexpr int TX = ztile<T>();
+    constexpr int NT = 256;
+    constexpr size_t sm = z_smem_bytes<T, NZ, TX>();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(z_kernel<T, NZ, TX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    z_kernel<T, NZ, TX, NT><<<dim3(ntiles, ninst), NT, sm, s>>>(d, a);
+    return cudaGetLastError();
+}
+
+#define CB_XY_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128)
+#define CB_Z_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+
+template <class T> bool Launch<T>::xy_supported(int nx) {
+    switch (nx) {
+#define CASE(n) case n: return XYCfg<T, n>::ok;
+        CB_XY_SIZES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+template <class T> bool Launch<T>::z_supported(int nz) {
+    switch (nz) {
+#define CASE(n) case n: return true;
+        CB_Z_SIZES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+template <class T> int Launch<T>::z_tile() { return ztile<T>(); }
+
+template <class T>
+cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    switch (nx) {
+#define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s);
+        CB_XY_SIZES(CASE)
+#undef CASE
+        default: return cudaErrorInvalidValue;
+    }
+}
+template <class T>
+cudaError_t Launch<T>::z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
+    switch (nz) {
+#define CASE(n) case n: return z_go<T, n>(d, ninst, ntiles, a, s);
+        CB_Z_SIZES(CASE)
+#undef CASE
+        default: return cudaErrorInvalidValue;
+    }
+}
+template <class T> cudaError_t Launch<T>::decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s) {
+    decide_kernel<T><<<(ninst + 127) / 128, 128, 0, s>>>(d, ninst, raw);
+    return cudaGetLastError();
+}
+template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s) {
+    coef_kernel<T><<<ninst, 512, 0, s>>>(d, accurate);
+    return cudaGetLastError();
+}
+template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out, size_t n, cudaStream_t s) {
+    const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    cplx_to_double_kernel<T><<<blocks, 256, 0, s>>>(reinterpret_cast<const cplx<T>*>(in), reinterpret_cast<double2*>(out), n);
+    return cudaGetLastError();
+}
+
+}  // namespace cb

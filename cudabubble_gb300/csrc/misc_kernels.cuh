@@ -1,0 +1,185 @@
+// Small kernels around the two FFT passes: ETD coefficient tables, the
+// on-device accept/reject decision, and the slow-path pointwise kernels the
+// field getters use.
+#pragma once
+#include <math.h>
+#include "cb_fft.cuh"
+#include "cb_inst.h"
+
+namespace cb {
+
+// phi_1..3(z) = sum_j z^j / (j+k)!  (Taylor for |z| < 1, closed forms otherwise)
+__device__ inline void phi123(double z, double& p1, double& p2, double& p3) {
+    if (fabs(z) < 1.0) {
+        double t1 = 0.0, t2 = 0.0, t3 = 0.0, zp = 1.0, f1 = 1.0, f2 = 2.0, f3 = 6.0;
+        for (int j = 0; j < 24; ++j) {
+            t1 += zp / f1;
+            t2 += zp / f2;
+            t3 += zp / f3;
+            zp *= z;
+            f1 *= (double)(j + 2);
+            f2 *= (double)(j + 3);
+            f3 *= (double)(j + 4);
+        }
+        p1 = t1; p2 = t2; p3 = t3;
+    } else {
+        const double ez = exp(z);
+        p1 = (ez - 1.0) / z;
+        p2 = (ez - 1.0 - z) / (z * z);
+        p3 = (ez - 1.0 - z - 0.5 * z * z) / (z * z * z);
+    }
+}
+
+// Builds the per-|k|^2 coefficient table for the current dt, once per dt.
+// L(k) follows Calc.cu:579-606 with c = -cx |k|^2 (kappa = 2, D = 1.5).
+// accurate == 0 evaluates the reference's own closed forms (Calc.cu:446-569);
+// accurate == 1 uses phi-functions, free of the small-|hL| cancellation.
+template <class T>
+__global__ void coef_kernel(const InstT<T>* __restrict__ insts, int accurate) {
+    const InstT<T>& I = insts[blockIdx.x];
+    Ctrl* ctrl = I.ctrl;
+    const Params& p = I.p;
+    if (p.method == M_EULER) return;
+    const double dt = ctrl->dt;
+    if (ctrl->dt_tab == dt) return;
+    const double kappa = 2.0, D = 1.5, eps = p.eps;
+    for (int idx = threadIdx.x; idx <= p.kmax; idx += blockDim.x) {
+        const double c = -(double)idx * p.cx;
+        const double L = -eps * c * c + kappa * c / eps + D * (c - kappa / (eps * eps)) / eps;
+        T* out = I.coef + 8 * (size_t)idx;
+        if (p.method == M_ETD2) {
+            double e1 = exp(L * dt), c1, c2;
+            if (accurate) {
+                double p1, p2, p3;
+                phi123(dt * L, p1, p2, p3);
+                c1 = dt * p1;
+                c2 = dt * p2;
+            } else {
+                c1 = (e1 - 1.0) / L;
+                c2 = (dt * L == 0.0) ? dt / 2 : (e1 - 1.0 - dt * L) / (dt * L * L);
+            }
+            out[0] = (T)e1; out[1] = (T)c1; out[2] = (T)c2;
+        } else {
+            const double eh = exp(L * dt / 2), e2 = eh * eh;
+            double ch, f1, f2, f3;
+            if (accurate) {
+                double p1, p2, p3;
+                phi123(dt * L / 2, p1, p2, p3);
+                ch = dt / 2 * p1;
+                phi123(dt * L, p1, p2, p3);
+                f1 = dt * (p1 - 3.0 * p2 + 4.0 * p3);
+                f2 = 2.0 * dt * (p2 - 2.0 * p3);
+                f3 = dt * (4.0 * p3 - p2);
+            } else {
+                const double h = dt;
+                const double q = 1.0 / (h * h * L * L * L);
+                ch = (eh - 1.0) / L;
+                f1 = q * (-4.0 - h * L + e2 * (4.0 - 3.0 * h * L + h * h * L * L));
+                f2 = q * 2.0 * (2.0 + h * L + e2 * (-2.0 + h * L));
+                f3 = q * (-4.0 - 3.0 * h * L - h * h * L * L + e2 * (4.0 - h * L));
+            }
+            out[0] = (T)eh; out[1] = (T)ch; out[2] = (T)e2; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) ctrl->dt_tab = dt;
+}
+
+// Accept / reject after one attempt (one thread per instance).
+//   adaptive: reject when E_new > E_old, halve dt (belastic.cpp:653-668 and :380-394);
+//             grow dt every grow_every accepted steps (belastic.cpp:644-651, :376-378)
+//   corr:     fixed dt with M != 0 -- correct alpha/beta and redo the step once
+//             from the kept state (belastic.cpp:670-691)
+//   raw:      accept unconditionally (a single reference step body)
+// Exit tests follow belastic.cpp:400-428 (Euler) and :712-740 (ETD).
+template <class T>
+__global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const InstT<T>& I = insts[i];
+    Ctrl* c = I.ctrl;
+    const Params& p = I.p;
+    if (c->done) return;
+    c->attempts++;
+    const Scal cs = c->sc[R_CAND];
+    const double E1 = cs.E;
+    c->E_last_attempt = E1;
+    if (!raw) {
+        if (p.adaptive) {
+            if (E1 > c->E_state) {
+                c->dt *= 0.5;
+                c->rejects++;
+                c->fresh = 0;
+                if (c->dt < p.dt_min) { c->done = 1; c->status = ST_DT_UNDERFLOW; }
+                return;
+            }
+        } else if (p.corr) {
+            c->alpha -= (cs.V - c->alpha0);
+            c->beta -= (cs.S - c->beta0);
+            if (c->corr_phase == 0) {
+                c->corr_phase = 1;
+                c->fresh = 1;  // N_u depends on alpha, beta
+                return;
+            }
+            c->corr_phase = 0;
+        }
+    }
+    // accept: the candidate becomes the state
+    const double E0 = c->E_state;
+    c->spec_state ^= 1;
+    c->part_state ^= 1;
+    c->sc[R_STATE] = cs;
+    c->E_state = E1;
+    c->fresh = 1;
+    const bool nonfinite = !isfinite(E1) || !isfinite(cs.V) || !isfinite(cs.S);
+    if (nonfinite) { c->done = 1; c->status = ST_NONFINITE; c->nonfinite = 1; return; }
+    if (!raw) {
+        if (p.method == M_EULER) {
+            if (c->t > p.tmax) { c->done = 1; c->status = ST_TMAX; return; }
+            if (cs.lsq * p.L3 < 1e-25) { c->done = 1; c->status = ST_CONVERGED; return; }
+        } else {
+            const double e0 = p.adaptive ? E0 : c->E_init;
+            if (e0 < 1e-3) { c->done = 1; c->status = ST_SMALL_ENERGY; return; }
+        }
+    }
+    c->t += c->dt;
+    c->steps++;
+    if (c->steps >= c->target) { c->done = 1; c->status = ST_TARGET; }
+    if (!raw && p.adaptive && c->steps % p.grow_every == 0)
+        c->dt = (c->dt * p.cap_probe < p.dt_cap) ? c->dt * p.grow_factor : p.dt_cap;
+}
+
+// ---------------------------------------------------------- slow path
+enum PwKind { PW_F = 0, PW_G0 = 1, PW_T = 2, PW_NLD = 3, PW_S = 4, PW_RHS = 5 };
+
+// Pointwise field getters on FP64 real arrays (Calc.cu:153-180, :265-284, :358-368, :410-419).
+static __global__ void pointwise_kernel(int kind, size_t n, double* out, const double* a, const double* b,
+                                 const double* c, const double* d, double eps, double x0, double x1, double x2) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double u = a[i];
+        switch (kind) {
+            case PW_F: out[i] = -b[i] * eps + (u * u - 1.0) * u / eps; break;                   // b = lap u
+            case PW_G0: out[i] = -c[i] + (3.0 * u * u - 1.0) * b[i] / (eps * eps); break;      // b = f, c = lap f
+            case PW_T: out[i] = u * (u * u - 1.0 - 2.0); break;
+            case PW_NLD: {                                                                     // b = f, c = t, d = lap t
+                const double ie = 1.0 / eps, ie2 = ie * ie, ie3 = ie * ie2, D = 1.5;
+                out[i] = -d[i] * ie + D * c[i] * ie3 + (3.0 * u * u - D - 1.0) * ie2 * b[i];
+                break;
+            }
+            case PW_S: {  // a = u, b, c, d = grad
+                const double g = b[i] * b[i] + c[i] * c[i] + d[i] * d[i];
+                out[i] = 0.5 * eps * g + 0.25 / eps * (u * u - 1.0) * (u * u - 1.0);
+                break;
+            }
+            case PW_RHS: out[i] = x0 * 0.5 + x1 * b[i] + c[i] * x2; break;                    // a unused, b = f, c = g0
+        }
+    }
+}
+
+template <class T>
+__global__ void cplx_to_double_kernel(const cplx<T>* __restrict__ in, double2* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+
+}  // namespace cb

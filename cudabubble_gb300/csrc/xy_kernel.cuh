@@ -1,0 +1,351 @@
+// xy-plane pass: one CTA owns one z-plane of one instance.
+//
+// Input is a "partial" plane (real z, spectral ky/kx) of the half spectrum:
+// P0 = IFFT_z(u-hat) and P2 = IFFT_z(-cx kz^2 u-hat).  In shared memory the
+// plane is packed to nx/2 complex columns: the kx = 0 and kx = nx/2 columns
+// are both Hermitian in ky, so they travel together as col0 + i*colN through
+// the y transform and come out as the real and imaginary parts.  The x
+// transform is a real transform done through a half-length complex FFT.
+//
+// Modes
+//   XY_REDUCE_FULL  u, lap u -> f; FP64 sums of u, (u^2-1)^2, f^2  (V, S, E_el, E)
+//   XY_REDUCE_S     u only; sums of u, (u^2-1)^2                    (V, S)
+//   XY_NONLIN       u, lap u -> pointwise nonlinearity G and H, forward xy
+//                   transforms, written as the partials A = G^ + beta cx (kx^2+ky^2) H^
+//                   and B = H^ that the z pass turns into the nonlinear spectrum
+//   XY_INV_PLAIN    partial -> real plane (double out)
+//   XY_FWD_PLAIN    real plane (double in) -> partial
+// The pointwise formulas restate Calc.cu:153-162 (f), :171-180 (g0),
+// :265-284 (nld), :358-368 (s), :410-437 (nld1/nld2).
+#pragma once
+#include "cb_fft.cuh"
+#include "cb_inst.h"
+#include "cb_kargs.h"
+
+namespace cb {
+
+template <class T> struct Acc;
+template <> struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+// FP32 values summed with Kahan compensation, handed to FP64 at the end
+template <> struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float y = x - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ int part_set(const Ctrl* ctrl, int role) {
+    return role == R_WORK ? 2 : (role == R_STATE ? ctrl->part_state : 1 - ctrl->part_state);
+}
+
+// Finalise the FP64 scalars of one state (phasefield.cpp:283-325,
+// belastic.cpp:68-86); run by one thread of the last CTA.
+__device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* part, int role, bool full) {
+    double su = 0.0, ss = 0.0, sf = 0.0;
+    for (int z = 0; z < p.nz; ++z) {
+        su += __ldcg(part + 4 * z + 0);
+        ss += __ldcg(part + 4 * z + 1);
+        sf += __ldcg(part + 4 * z + 2);
+    }
+    Scal& s = ctrl->sc[role];
+    const double c3 = 3.0 / (2.0 * sqrt(2.0));
+    s.sum_u = su;
+    s.sum_s2 = ss;
+    s.V = (su * p.invN + 1.0) * 0.5 * p.L3;
+    s.S = (0.5 * p.eps * s.grad2 + 0.25 / p.eps * (ss * p.invN)) * c3 * p.L3;
+    if (full) {
+        s.sum_f2 = sf;
+        s.E_el = (sf * p.invN) * (1.0 / (p.eps * 2.0)) * p.L3;
+        const double ve = s.V - ctrl->alpha, se = s.S - ctrl->beta;
+        s.E = p.eta * s.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
+    }
+}
+
+template <class T, int NX, int NT>
+__global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
+    using C = cplx<T>;
+    constexpr int M = NX / 2, NY = NX, NC = M + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const InstT<T>& I = insts[blockIdx.y];
+    Ctrl* ctrl = I.ctrl;
+    const Params& p = I.p;
+    const int z = blockIdx.x;
+    const int tid = threadIdx.x;
+    if (z >= p.nz) return;
+    const bool stepping = a.mode <= XY_NONLIN;
+    if (stepping) {
+        if (ctrl->done) return;
+        if (a.skip_if_stale && !ctrl->fresh) return;
+    }
+    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
+    const int pitch = nf * M + 1;
+    C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
+    C* twM = S + NY * pitch;                // W_M^m
+    C* twN = twM + M;                       // W_NX^m
+    C* twY = twN + NX;                      // W_NY^m
+    double* red = reinterpret_cast<double*>(twY + NY);
+
+    {
+        const C* gx = reinterpret_cast<const C*>(I.twx);
+        const C* gy = reinterpret_cast<const C*>(I.twy);
+        for (int i = tid; i < M + NX; i += NT) twM[i] = gx[i];  // twM and twN are contiguous
+        for (int i = tid; i < NY; i += NT) twY[i] = gy[i];
+    }
+    const T cx = (T)p.cx;
+    const size_t plane = (size_t)NY * NC;
+
+    if (a.mode == XY_FWD_PLAIN) {
+        // real plane in natural order -> transposed slots, as the TN transforms expect
+        const double* src = a.rin + (size_t)z * NY * NX;
+        for (int it = tid; it < NY * M; it += NT) {
+            const int m = it % M, y = it / M;
+            const double2 v = reinterpret_cast<const double2*>(src + (size_t)y * NX)[m];
+            S[tpos<NY>(y) * pitch + tpos<M>(m)] = cmk<C>((T)v.x, (T)v.y);
+        }
+        __syncthreads();
+    } else {
+        const C* P0;
+        const C* P2 = nullptr;
+        if (a.mode == XY_INV_PLAIN) {
+            P0 = reinterpret_cast<const C*>(a.cin) + (size_t)z * plane;
+        } else {
+            const int set = part_set(ctrl, a.role);
+            P0 = reinterpret_cast<const C*>(I.P[set][0]) + (size_t)z * plane;
+            P2 = reinterpret_cast<const C*>(I.P[set][1]) + (size_t)z * plane;
+        }
+        for (int it = tid; it < NY * M; it += NT) {
+            const int c = it % M, ky = it / M;
+            const C v = P0[ky * NC + c];
+            C vN = cmk<C>(0, 0);
+            if (c == 0) {
+                vN = P0[ky * NC + M];
+                S[ky * pitch] = cmk<C>(v.x - vN.y, v.y + vN.x);  // col0 + i*colN
+            } else {
+                S[ky * pitch + c] = v;
+            }
+            if (nf == 2) {  // laplacian partial Q = -cx (kx^2 + ky^2) P0 + P2 (Calc.cu:107-124)
+                const int kyf = min(ky, NY - ky);
+                const T kyy = cx * (T)(kyf * kyf);
+                const C w = P2[ky * NC + c];
+                if (c == 0) {
+                    const C wN = P2[ky * NC + M];
+                    const T kN = cx * (T)(M * M) + kyy;
+                    const C q0 = cmk<C>(w.x - kyy * v.x, w.y - kyy * v.y);
+                    const C qN = cmk<C>(wN.x - kN * vN.x, wN.y - kN * vN.y);
+                    S[ky * pitch + M] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
+                } else {
+                    const T k2 = cx * (T)(c * c) + kyy;
+                    S[ky * pitch + M + c] = cmk<C>(w.x - k2 * v.x, w.y - k2 * v.y);
+                }
+            }
+        }
+        __syncthreads();
+        // ---- y inverse (natural in, transposed out) on nf*M columns
+        fft_lines_NT<NY, true, NT>(S, nf * M, LinearLines{1}, pitch, twY);
+        __syncthreads();
+        // ---- x C2R: half-length pre-processing, then inverse M-point FFT per row
+        const PairRows rows{NY, pitch, M};
+        for (int it = tid; it < nf * NY * (M / 2 + 1); it += NT) {
+            const int l = it % (nf * NY), k = it / (nf * NY);
+            C* row = S + rows(l);
+            if (k == 0) {
+                const C v = row[0];  // X[0] + i X[M], both real
+                row[0] = cmk<C>(v.x + v.y, v.x - v.y);
+            } else {
+                const int k2 = M - k;
+                const C xk = row[k], xk2 = row[k2];
+                {
+                    const C e = cadd(xk, cconj(xk2));
+                    const C o = cmulc(csub(xk, cconj(xk2)), twN[k]);  // * W_N^{-k}
+                    row[k] = cmk<C>(e.x - o.y, e.y + o.x);            // e + i o
+                }
+                if (k2 != k) {
+                    const C e = cadd(xk2, cconj(xk));
+                    const C o = cmulc(csub(xk2, cconj(xk)), twN[k2]);
+                    row[k2] = cmk<C>(e.x - o.y, e.y + o.x);
+                }
+            }
+        }
+        __syncthreads();
+        fft_lines_NT<M, true, NT>(S, nf * NY, rows, 1, twM);
+        __syncthreads();
+
+        if (a.mode == XY_INV_PLAIN) {
+            double* dst = a.rout + (size_t)z * NY * NX;
+            for (int it = tid; it < NY * M; it += NT) {
+                const int m = it % M, y = it / M;
+                const C v = S[tpos<NY>(y) * pitch + tpos<M>(m)];
+                reinterpret_cast<double2*>(dst + (size_t)y * NX)[m] = make_double2((double)v.x, (double)v.y);
+            }
+            return;
+        }
+
+        // ---- pointwise over all slots (order-free)
+        const T eps = (T)p.eps, ieps = (T)(1.0 / p.eps), ieps2 = (T)(1.0 / (p.eps * p.eps)),
+                ieps3 = (T)(1.0 / (p.eps * p.eps * p.eps));
+        if (a.mode == XY_NONLIN) {
+            const Scal& sc = ctrl->sc[a.role];
+            const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
+            const T eta = (T)p.eta;
+            const T kappa = (T)2.0, D = (T)1.5;  // phasefield.cpp:259-260
+            const bool euler = p.method == M_EULER;
+            // ETD  (Calc.cu:428-437 with nld from :265-284):
+            //   G = -lam1/2 - c3 lam2 f - eta (D t / eps^3 + (3u^2 - D - 1) f / eps^2),  H = t
+            // Euler (Calc.cu:410-419 with g0 from :171-180):
+            //   G = lam1/2 + lam2 f + eta (3u^2 - 1) f / eps^2,                         H = f
+            const T g_c = euler ? (T)(0.5 * lam1) : (T)(-0.5 * lam1);
+            const T g_f = euler ? (T)lam2 : (T)(-lam2 * 3.0 / (2.0 * sqrt(2.0)));
+            for (int it = tid; it < NY * M; it += NT) {
+                const int q = it % M, r = it / M;
+                C* pu = S + r * pitch + q;
+                C* pl = pu + M;
+                const C uu = *pu, ll = *pl;
+                T gv[2], hv[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const T u = e ? uu.y : uu.x, lap = e ? ll.y : ll.x;
+                    const T u2 = u * u;
+                    const T f = -lap * eps + (u2 - (T)1) * u * ieps;
+                    if (euler) {
+                        gv[e] = g_c + g_f * f + eta * ((T)3 * u2 - (T)1) * f * ieps2;
+                        hv[e] = f;
+                    } else {
+                        const T t = u * (u2 - (T)1 - kappa);
+                        gv[e] = g_c + g_f * f - eta * (D * t * ieps3 + ((T)3 * u2 - D - (T)1) * ieps2 * f);
+                        hv[e] = t;
+                    }
+                }
+                *pu = cmk<C>(gv[0], gv[1]);
+                *pl = cmk<C>(hv[0], hv[1]);
+            }
+            __syncthreads();
+        } else {
+            // reductions (XY_REDUCE_FULL / XY_REDUCE_S)
+            const bool full = a.mode == XY_REDUCE_FULL;
+            Acc<T> au, as, af;
+            for (int it = tid; it < NY * M; it += NT) {
+                const int q = it % M, r = it / M;
+                const C uu = S[r * pitch + q];
+                const C ll = full ? S[r * pitch + M + q] : cmk<C>(0, 0);
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const T u = e ? uu.y : uu.x;
+                    const T u2m = u * u - (T)1;
+                    au.add(u);
+                    as.add(u2m * u2m);
+                    if (full) {
+                        const T lap = e ? ll.y : ll.x;
+                        const T f = -lap * eps + u2m * u * ieps;
+                        af.add(f * f);
+                    }
+                }
+            }
+            double v[3] = {au.get(), as.get(), af.get()};
+            block_sum<3>(v, red);
+            double* part = I.part_xy;
+            if (tid == 0) {
+                part[4 * z + 0] = v[0];
+                part[4 * z + 1] = v[1];
+                part[4 * z + 2] = v[2];
+                __threadfence();
+                const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[a.role], 1u);
+                if (done_blocks == (unsigned)(p.nz - 1)) {
+                    __threadfence();
+                    finalize_xy(p, ctrl, part, a.role, full);
+                    ctrl->cnt_xy[a.role] = 0u;
+                }
+            }
+            return;
+        }
+    }
+
+    // ---- forward xy: x R2C (transposed in, natural out) then y (transposed in, natural out)
+    const int nfo = (a.mode == XY_NONLIN) ? 2 : 1;
+    const PairRows rows{NY, pitch, M};
+    fft_lines_TN<M, false, NT>(S, nfo * NY, rows, 1, twM);
+    __syncthreads();
+    for (int it = tid; it < nfo * NY * (M / 2 + 1); it += NT) {
+        const int l = it % (nfo * NY), k = it / (nfo * NY);
+        C* row = S + rows(l);
+        if (k == 0) {
+            const C z0 = row[0];
+            row[0] = cmk<C>(z0.x + z0.y, z0.x - z0.y);  // X[0] + i X[M]
+        } else {
+            const int k2 = M - k;
+            const C zk = row[k], zk2 = row[k2];
+            const T h = (T)0.5;
+            {
+                const C e = cadd(zk, cconj(zk2));
+                const C d = cmul(csub(zk, cconj(zk2)), twN[k]);
+                row[k] = cmk<C>(h * (e.x + d.y), h * (e.y - d.x));  // (e - i d) / 2
+            }
+            if (k2 != k) {
+                const C e = cadd(zk2, cconj(zk));
+                const C d = cmul(csub(zk2, cconj(zk)), twN[k2]);
+                row[k2] = cmk<C>(h * (e.x + d.y), h * (e.y - d.x));
+            }
+        }
+    }
+    __syncthreads();
+    fft_lines_TN<NY, false, NT>(S, nfo * M, LinearLines{1}, pitch, twY);
+    __syncthreads();
+
+    // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
+    C* outA;
+    C* outB = nullptr;
+    if (a.mode == XY_NONLIN) {
+        outA = reinterpret_cast<C*>(I.A) + (size_t)z * plane;
+        outB = reinterpret_cast<C*>(I.B) + (size_t)z * plane;
+    } else {
+        outA = reinterpret_cast<C*>(a.cout) + (size_t)z * plane;
+    }
+    const T bnl = (T)((p.method == M_EULER) ? p.eta : -p.eta / p.eps) * cx;
+    for (int it = tid; it < NY * M; it += NT) {
+        const int c = it % M, ky = it / M;
+        const C zg = S[ky * pitch + c];
+        const int kyf = min(ky, NY - ky);
+        if (c == 0) {
+            const int kym = (NY - ky) % NY;
+            const C zg2 = S[kym * pitch];
+            const T h = (T)0.5;
+            const C g0 = cmk<C>(h * (zg.x + zg2.x), h * (zg.y - zg2.y));
+            const C gN = cmk<C>(h * (zg.y + zg2.y), h * (zg2.x - zg.x));  // -i/2 (z - conj z2)
+            if (outB) {
+                const C zh = S[ky * pitch + M], zh2 = S[kym * pitch + M];
+                const C h0 = cmk<C>(h * (zh.x + zh2.x), h * (zh.y - zh2.y));
+                const C hN = cmk<C>(h * (zh.y + zh2.y), h * (zh2.x - zh.x));
+                const T m0 = bnl * (T)(kyf * kyf), mN = bnl * (T)(M * M + kyf * kyf);
+                outA[ky * NC] = cmk<C>(g0.x + m0 * h0.x, g0.y + m0 * h0.y);
+                outA[ky * NC + M] = cmk<C>(gN.x + mN * hN.x, gN.y + mN * hN.y);
+                outB[ky * NC] = h0;
+                outB[ky * NC + M] = hN;
+            } else {
+                outA[ky * NC] = g0;
+                outA[ky * NC + M] = gN;
+            }
+        } else {
+            if (outB) {
+                const C zh = S[ky * pitch + M + c];
+                const T mm = bnl * (T)(c * c + kyf * kyf);
+                outA[ky * NC + c] = cmk<C>(zg.x + mm * zh.x, zg.y + mm * zh.y);
+                outB[ky * NC + c] = zh;
+            } else {
+                outA[ky * NC + c] = zg;
+            }
+        }
+    }
+}
+
+template <class T, int NX> constexpr size_t xy_smem_bytes(int nf) {
+    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + NX / 2 + NX + NX) + 32 * 4 * sizeof(double);
+}
+
+}  // namespace cb

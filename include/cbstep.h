@@ -1,0 +1,166 @@
+/* cbstep.h -- C ABI of the GB300 pseudo-spectral Allen-Cahn stepper.
+ *
+ * Drop-in replacement for the per-step call surface of CudaBubble's
+ * vesicle relaxation (phase-field elastic bending energy with volume and
+ * surface-area penalties on a periodic [-pi, pi]^3 grid).  The reference has
+ * no plugin or FFI layer; it is one executable whose time loops call
+ * (citations are file:line in the reference tree):
+ *
+ *   belastic::ETD2RK(Het)              belastic.cpp:491-517   -> cb_ETD2RK
+ *   belastic::ETD4RK(Het)              belastic.cpp:519-552   -> cb_ETD4RK
+ *   get_sum_fgqterm + time_diff_solve_phi
+ *                                      belastic.cpp:52-64, phasefield.cpp:89-93
+ *                                                             -> cb_euler_step
+ *   belastic::getstaticenergy          belastic.cpp:68-86     -> cb_getstaticenergy
+ *   belastic::run_static   (Euler)     belastic.cpp:286-470   -> cb_run (method CB_EULER)
+ *   belastic::run_static_fEIF (ETD)    belastic.cpp:554-786   -> cb_run (CB_ETD2 / CB_ETD4)
+ *   phasefield getters fd/lap/f/g0/nld/gradient/s/vol/surface/elastic_eng
+ *                                      phasefield.cpp:130-325 -> cb_field, cb_scalars
+ *   fluidbase ini first line (34 fields)
+ *                                      fluidbase.cpp:33-35    -> cb_params_from_ini_line
+ *
+ * Conventions: real fields are double[nz][ny][nx] with x fastest (the
+ * reference's .out layout, tool.cpp:118-132); spectra are complex double
+ * [nz][ny][nx/2+1] (cuFFT D2Z layout, forward-normalised by 1/N as in
+ * Calc.cu:88-96).  Every call returns CB_OK or a negative CB_E* code and
+ * never exits the process (the reference exit()s, Calc.cu:52-55).
+ * A handle owns one CUDA stream; calls on one handle are not thread-safe.
+ */
+#ifndef CBSTEP_H
+#define CBSTEP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    CB_OK = 0,
+    CB_EINVAL = -1,         /* bad argument or unsupported grid */
+    CB_ENOMEM = -2,         /* device allocation failed / over budget */
+    CB_ECUDA = -3,          /* CUDA runtime error (see cb_last_error) */
+    CB_ENONFINITE = -4,     /* the state blew up (non-finite energy) */
+    CB_ENOTCONVERGED = -5,  /* step / attempt limit reached */
+    CB_ETIMEOUT = -6,       /* a bounded wait ran out */
+    CB_EDTUNDERFLOW = -7,   /* adaptive dt fell below 1e-23 (belastic.cpp:713) */
+    CB_EUNSUPPORTED = -8    /* combination not built (grid size / precision) */
+};
+
+enum { CB_EULER = 0, CB_ETD2 = 1, CB_ETD4 = 2 };
+enum { CB_FP64 = 0, CB_FP32 = 1 };
+
+/* exit reasons reported in cb_scalars.status */
+enum {
+    CB_RUNNING = 0, CB_DONE_TARGET = 1, CB_DONE_DT_UNDERFLOW = 2, CB_DONE_SMALL_ENERGY = 3,
+    CB_DONE_NONFINITE = 4, CB_DONE_CONVERGED = 5, CB_DONE_TMAX = 6
+};
+
+/* field selectors for cb_field (phasefield.cpp getters) */
+enum {
+    CB_FIELD_PHI = 0,     /* phi (real)                              phasefield::d        */
+    CB_FIELD_FD = 1,      /* phi-hat (complex, half spectrum)        phasefield::fd       */
+    CB_FIELD_LAP = 2,     /* lap phi                                 phasefield::lap      */
+    CB_FIELD_F = 3,       /* f = -eps lap phi + (phi^2-1) phi / eps  phasefield::f        */
+    CB_FIELD_G0 = 4,      /* g0 = -lap f + (3 phi^2 - 1) f / eps^2   phasefield::g0       */
+    CB_FIELD_NLD = 5,     /* ETD nonlinearity                        phasefield::nld      */
+    CB_FIELD_DX = 6,      /* spectral gradient, Nyquist zeroed       phasefield::gradient */
+    CB_FIELD_DY = 7,
+    CB_FIELD_DZ = 8,
+    CB_FIELD_S = 9,       /* surface density                         phasefield::s        */
+    CB_FIELD_NLD_HAT = 10,/* N-hat of the ETD step (complex)         belastic::get_nld_term   (ETD handles) */
+    CB_FIELD_RHS = 11     /* Euler right-hand side (real)            belastic::get_sum_fgqterm (Euler handles) */
+};
+
+typedef struct cb_params {
+    int nx, ny, nz;          /* ny is forced to nx, as Calc.cu:45-46 does; nx even */
+    double lenx;             /* box edge in units of 2*pi (ini "lenx", fluidbase.cpp:52-57) */
+    int epssize;             /* ini "epssize": eps rule of fluidbase.cpp:68-108 */
+    double eps;              /* > 0 overrides the epssize rule */
+    double eta, ga;          /* bending rigidity, Euler mobility */
+    double alpha, beta;      /* volume / area targets; beta <= 0: take them from t = 0 */
+    double M1, M2;           /* volume / area penalty coefficients */
+    double time_step;        /* initial dt */
+    double fixed_time_step;  /* > 0: fixed dt = min(fixed_time_step, time_step) */
+    double tmax;             /* Euler loop time limit */
+    int method;              /* CB_EULER / CB_ETD2 / CB_ETD4 */
+    int precision;           /* CB_FP64 (plain form) / CB_FP32 (FP32 FFT + FP64 reductions) */
+    /* adaptive-dt schedule; defaults reproduce belastic.cpp:644-651 (ETD) and :376-378 (Euler) */
+    int grow_every;          /* 0: method default (4) */
+    double grow_factor;      /* 0: method default (2.0 ETD, 1.4 Euler) */
+    double dt_cap;           /* 0: method default (1e-3 ETD, none for Euler) */
+    double cap_probe;        /* 0: method default (1.4 ETD) */
+    int etd4_textbook;       /* 1: Cox-Matthews combine with N_u; 0: the reference's N_a (belastic.cpp:550) */
+    int accurate_coefficients; /* -1: default (FP32 form: phi-function series; FP64 form: reference closed forms) */
+} cb_params;
+
+typedef struct cb_scalars {
+    double V, S, E_el, E;    /* volume, area, elastic energy, total static energy */
+    double lamb1, lamb2;     /* M1 (V - alpha), M2 (S - beta) */
+    double alpha, beta;
+    double dt, t;
+    double lserror;          /* Euler LSerror of the last step (belastic.cpp:414) */
+    int steps, attempts, rejects, status;
+} cb_scalars;
+
+typedef struct cb_run_stats {
+    int steps;               /* accepted steps taken by this call */
+    int attempts;            /* attempts (accepted + rejected) */
+    int status;              /* CB_DONE_* exit reason */
+    int graph_launches;
+    double device_ms;        /* CUDA-event time of the call's device work */
+} cb_run_stats;
+
+typedef struct cb_handle cb_handle;
+
+/* defaults for every field (FP64 ETD4 on 64^3, the reference's main path) */
+void cb_params_default(cb_params* p);
+/* parse the reference's ini first line (fluidbase.cpp:33-35 field order and
+ * defaults); an optional 35th field selects the method and a 36th the
+ * precision.  Returns CB_OK or CB_EINVAL. */
+int cb_params_from_ini_line(const char* line, cb_params* p);
+/* eps the instance will use (fluidbase.cpp:68-108) */
+double cb_params_eps(const cb_params* p);
+/* HBM bytes one instance needs */
+long long cb_instance_bytes(const cb_params* p);
+/* 1 when the (grid, precision, method) combination is built */
+int cb_supported(const cb_params* p);
+
+int cb_create(const cb_params* p, cb_handle** out);
+int cb_destroy(cb_handle* h);
+/* phi in the .out layout; on_device != 0 means a device pointer */
+int cb_set_phi(cb_handle* h, const double* phi, int on_device);
+int cb_get_phi(cb_handle* h, double* phi, int on_device);
+int cb_scalars_get(cb_handle* h, cb_scalars* s);
+double cb_getstaticenergy(cb_handle* h);
+/* single reference step bodies at the current dt, always accepted */
+int cb_ETD2RK(cb_handle* h);
+int cb_ETD4RK(cb_handle* h);
+int cb_euler_step(cb_handle* h);
+/* the reference time loop of the handle's method until nsteps more accepted steps */
+int cb_run(cb_handle* h, int nsteps, cb_run_stats* st);
+/* derived fields; real fields N doubles, complex fields 2*Nc doubles */
+int cb_field(cb_handle* h, int which, double* out, int on_device);
+/* set the time step (and drop the cached coefficient table) */
+int cb_set_dt(cb_handle* h, double dt);
+int cb_synchronize(cb_handle* h);
+/* HBM bytes held by the handle's stepping state */
+long long cb_handle_bytes(cb_handle* h);
+
+/* ---- measurement (no counterpart in the reference) ------------------------
+ * cb_run_timed: cb_run, but one attempt per CUDA-event pair on the handle's
+ * stream; flush_bytes > 0 writes that many bytes between attempts (outside
+ * the timed pairs) so every attempt starts with a cold L2.  device_ms is the
+ * summed attempt time.
+ * cb_profile_kernels: nattempts loop attempts launched kernel by kernel with
+ * an event pair around each launch; ms[k] / counts[k] per kernel kind
+ * k = 0 xy nonlinear pass, 1 xy reduce (S only), 2 xy reduce (full),
+ * 3 z pass, 4 decide + coefficient table. */
+int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts);
+int cb_profile_kernels(cb_handle* h, int nattempts, long long flush_bytes, double* ms, int* counts);
+
+const char* cb_last_error(void);
+const char* cb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CBSTEP_H */

@@ -1,0 +1,120 @@
+"""GPU parity of every derived field and single step body against the FP64
+oracle (oracle/oracle.py), through the C ABI.
+
+Tolerances: the plain FP64 form must agree to FP64 round-off (1e-11 of the
+field's max magnitude); the FP32 form (FP32 FFT and pointwise math, FP64
+reductions) to 2e-5 of the field's max magnitude for fields and 1e-6
+relative for the FP64-reduced scalars V, S, E.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (nx, nz, epssize, axes-seed)
+    (16, 16, 200, None),
+    (24, 24, 150, 11),
+    (32, 16, 150, 12),
+    (48, 48, 150, 2),
+    (64, 64, 200, None),
+]
+
+
+def _phi0(nx, nz, es, seed):
+    from cudabubble_gb300 import shapes
+    eps = shapes.eps_rule(es, nx)
+    if seed is None:
+        return shapes.ellipsoid(nx, nz, eps, (1.6, 1.6, 0.8))
+    return shapes.seeded_ellipsoid(nx, nz, eps, seed)
+
+
+def _oracle(nx, nz, es, phi0, dt, method="etd2"):
+    eps = O.eps_from_epssize(es, 2 * math.pi, nx)
+    p = O.Params(nx=nx, nz=nz, eps=eps, time_step=dt, fixed_time_step=dt)
+    b = O.Belastic(p, phi0)
+    b.set_alpha_beta_from_t0()
+    return b
+
+
+def _handle(cblib, nx, nz, es, method, prec, dt, phi0):
+    from cudabubble_gb300 import capi
+    p = capi.default_params(nx=nx, ny=nx, nz=nz, epssize=es, method=method, precision=prec, time_step=dt,
+                            fixed_time_step=dt, M1=1e4, M2=1e4)
+    st = capi.Stepper(p)
+    st.set_phi(phi0)
+    return st
+
+
+def _close(a, b, tol):
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(a - b).max() / scale
+    assert err <= tol, f"max rel-to-max error {err:.3e} > {tol:.1e}"
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}" for c in CASES])
+def test_fields_and_scalars(cblib, case, prec):
+    from cudabubble_gb300 import capi
+    nx, nz, es, seed = case
+    if prec == 0 and nx > 96:
+        pytest.skip("FP64 plane pass holds nx <= 96")
+    phi0 = _phi0(nx, nz, es, seed)
+    b = _oracle(nx, nz, es, phi0, 1e-6)
+    st = _handle(cblib, nx, nz, es, capi.CB_ETD2, prec, 1e-6, phi0)
+    tol = 1e-11 if prec == 0 else 2e-5
+    pd = b.pd
+    _close(st.get_phi(), pd.d, tol)
+    _close(st.field(capi.CB_FIELD_FD), pd.fd(), tol)
+    _close(st.field(capi.CB_FIELD_LAP), pd.lap(), tol)
+    _close(st.field(capi.CB_FIELD_F), pd.f(), 10 * tol)
+    _close(st.field(capi.CB_FIELD_G0), pd.g0(), 10 * tol)
+    _close(st.field(capi.CB_FIELD_NLD), pd.nld(), 10 * tol)
+    dx, dy, dz = pd.gradient()
+    _close(st.field(capi.CB_FIELD_DX), dx, tol)
+    _close(st.field(capi.CB_FIELD_DY), dy, tol)
+    _close(st.field(capi.CB_FIELD_DZ), dz, tol)
+    _close(st.field(capi.CB_FIELD_S), pd.s(), 10 * tol)
+    s = st.scalars()
+    stol = 1e-12 if prec == 0 else 1e-6
+    for k, ref in (("V", pd.vol()), ("S", pd.surface()), ("E_el", pd.elastic_eng()),
+                   ("E", b.getstaticenergy(pd))):
+        assert abs(s[k] - ref) <= stol * abs(ref), (k, s[k], ref)
+    # N-hat of the ETD step (belastic.cpp:473-489) through the hot-path kernels
+    _close(st.field(capi.CB_FIELD_NLD_HAT), b.get_nld_term(pd), 10 * tol)
+    st.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES[:4], ids=[f"{c[0]}x{c[1]}" for c in CASES[:4]])
+@pytest.mark.parametrize("method", ["euler", "etd2", "etd4"])
+def test_single_step(cblib, case, prec, method):
+    from cudabubble_gb300 import capi
+    nx, nz, es, seed = case
+    phi0 = _phi0(nx, nz, es, seed)
+    dt = {"euler": 1e-7, "etd2": 2e-6, "etd4": 1e-6}[method]
+    b = _oracle(nx, nz, es, phi0, dt)
+    m = {"euler": capi.CB_EULER, "etd2": capi.CB_ETD2, "etd4": capi.CB_ETD4}[method]
+    st = _handle(cblib, nx, nz, es, m, prec, dt, phi0)
+    if method == "euler":
+        R = b.get_sum_fgqterm(b.pd)
+        _close(st.field(capi.CB_FIELD_RHS), R, 1e-10 if prec == 0 else 1e-4)
+        b.euler_update(R)
+        st.euler_step()
+    elif method == "etd2":
+        b.init_fEIF()
+        b.ETD2RK()
+        st.ETD2RK()
+    else:
+        b.init_fEIF()
+        b.ETD4RK()
+        st.ETD4RK()
+    phi = st.get_phi()
+    err = np.abs(phi - b.pd.d).max()
+    assert err <= (1e-11 if prec == 0 else 2e-6), err
+    s = st.scalars()
+    assert abs(s["E"] - b.getstaticenergy(b.pd)) <= (1e-10 if prec == 0 else 1e-6) * abs(s["E"])
+    st.close()

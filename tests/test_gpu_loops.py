@@ -1,0 +1,62 @@
+"""GPU parity of the reference time loops (accept/reject, adaptive dt, the
+alpha/beta correction) against the FP64 oracle's restatement of
+belastic.cpp:286-470 and :554-786, through the C ABI.
+
+FP64 form: the accepted-step count, rejection count and final dt must match
+exactly and max|phi - phi_ref| <= 1e-10.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+LOOPS = [
+    # name, method, n, epssize, time_step, fixed, nsteps, seed
+    ("euler_fixed", "euler", 32, 200, 1e-7, 1e-7, 30, None),
+    ("euler_adapt", "euler", 32, 200, 1e-7, 0.0, 20, None),
+    ("etd2_adapt", "etd2", 32, 150, 1e-6, 0.0, 30, 2),
+    ("etd2_fixed_corr", "etd2", 24, 150, 1e-6, 1e-6, 10, 11),
+    ("etd4_fixed_corr", "etd4", 32, 150, 1e-6, 1e-6, 8, 3),
+    ("etd4_adapt", "etd4", 24, 150, 1e-6, 0.0, 16, 3),
+]
+
+
+def _phi0(n, es, seed):
+    from cudabubble_gb300 import shapes
+    eps = shapes.eps_rule(es, n)
+    return shapes.ellipsoid(n, n, eps, (1.6, 1.6, 0.8)) if seed is None else shapes.seeded_ellipsoid(n, n, eps, seed)
+
+
+@pytest.mark.parametrize("case", LOOPS, ids=[c[0] for c in LOOPS])
+def test_loop_fp64(cblib, case):
+    from cudabubble_gb300 import capi
+    name, method, n, es, ts, fixed, nsteps, seed = case
+    phi0 = _phi0(n, es, seed)
+    eps = O.eps_from_epssize(es, 2 * math.pi, n)
+    b = O.Belastic(O.Params(nx=n, nz=n, eps=eps, time_step=ts, fixed_time_step=fixed), phi0)
+    if method == "euler":
+        why = b.run_static(nsteps)
+    else:
+        why = b.run_static_fEIF(nsteps, method)
+    m = {"euler": capi.CB_EULER, "etd2": capi.CB_ETD2, "etd4": capi.CB_ETD4}[method]
+    p = capi.default_params(nx=n, ny=n, nz=n, epssize=es, method=m, precision=capi.CB_FP64, time_step=ts,
+                            fixed_time_step=fixed)
+    st = capi.Stepper(p)
+    st.set_phi(phi0)
+    r = st.run(nsteps)
+    s = st.scalars()
+    assert why == "max_steps"
+    assert s["steps"] == b.steps == nsteps
+    assert s["rejects"] == b.rejects
+    assert s["dt"] == pytest.approx(b.time_step, rel=1e-15)
+    assert s["alpha"] == pytest.approx(b.alpha, rel=1e-12)
+    assert s["beta"] == pytest.approx(b.beta, rel=1e-12)
+    err = np.abs(st.get_phi() - b.pd.d).max()
+    assert err <= 1e-10, err
+    assert s["E"] == pytest.approx(b.getstaticenergy(b.pd), rel=1e-11)
+    assert r["steps"] == nsteps
+    st.close()

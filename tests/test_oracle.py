@@ -1,0 +1,198 @@
+"""CPU checks of the oracle itself: analytic identities, the C port against
+the NumPy restatement, and both pinned to the reference's own outputs
+(tests/golden, produced by tests/golden/make_golden.py from the reference's
+FP64 cuFFT build)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MANIFEST = os.path.join(GOLDEN, "manifest.json")
+
+
+def _grid(n):
+    x = O.grid_coords(n, 2 * math.pi)
+    return x[None, None, :], x[None, :, None], x[:, None, None]
+
+
+def test_spectral_derivatives_of_modes_are_exact():
+    n = 32
+    c = O.Calc(n, n, 2 * math.pi)
+    X, Y, Z = _grid(n)
+    u = np.sin(2 * X) * np.cos(3 * Y) + np.cos(Z)
+    assert np.abs(c.lap(u) - (-13 * np.sin(2 * X) * np.cos(3 * Y) - np.cos(Z))).max() < 1e-12
+    dx, dy, dz = c.fftgradient(c.r2c_3d_f(u))
+    assert np.abs(dx - 2 * np.cos(2 * X) * np.cos(3 * Y)).max() < 1e-12
+    assert np.abs(dy + 3 * np.sin(2 * X) * np.sin(3 * Y)).max() < 1e-12
+    assert np.abs(dz + np.sin(Z)).max() < 1e-12
+
+
+def test_nyquist_conventions():
+    """Laplacian keeps the Nyquist mode (Calc.cu:117-119); the gradient zeroes it (Calc.cu:311-332)."""
+    n = 16
+    c = O.Calc(n, n, 2 * math.pi)
+    X, _, _ = _grid(n)
+    u = np.cos(8 * X) * np.ones((n, n, n))
+    assert np.abs(c.lap(u) + 64 * u).max() < 1e-12
+    assert np.abs(c.fftgradient(c.r2c_3d_f(u))[0]).max() == 0.0
+
+
+def test_volume_and_flat_energy():
+    n = 16
+    c = O.Calc(n, n, 2 * math.pi)
+    assert c.intf(np.ones(c.shape), 1.0, 0.5) == pytest.approx((2 * math.pi) ** 3, rel=1e-15)
+    pf = O.PhaseField(c, 0.3, np.ones(c.shape))
+    assert pf.elastic_eng() == 0.0 and pf.surface() == 0.0
+
+
+def test_single_mode_etd_closed_form():
+    """With M = 0 and a state whose nonlinear term vanishes (phi = 1 is a fixed
+    point: f = 0, t-term constant), ETD steps keep phi = 1 exactly."""
+    n = 16
+    eps = 0.4
+    b = O.Belastic(O.Params(nx=n, nz=n, eps=eps, M1=0.0, M2=0.0, time_step=1e-3, fixed_time_step=1e-3),
+                   np.ones((n, n, n)))
+    b.init_fEIF()
+    b.ETD2RK()
+    assert np.abs(b.pd.d - 1.0).max() < 1e-12
+
+
+def test_phi_function_coefficients_match_closed_forms_where_well_conditioned():
+    z = np.array([-0.3, -1.5, -7.0, -50.0])
+    p1, p2, p3 = O.phi123(z)
+    e = np.exp(z)
+    assert np.allclose(p1, (e - 1) / z, rtol=1e-14, atol=0)
+    assert np.allclose(p2, (e - 1 - z) / z ** 2, rtol=1e-13, atol=0)
+    f1 = (-4 - z + e * (4 - 3 * z + z * z)) / z ** 3
+    assert np.allclose(f1, p1 - 3 * p2 + 4 * p3, rtol=1e-12, atol=0)
+
+
+@pytest.fixture(scope="module")
+def cstep():
+    from oracle import cbuild
+    cbuild.build()
+    return cbuild
+
+
+@pytest.mark.parametrize("n,nz", [(16, 16), (24, 24), (32, 16), (48, 48)])
+def test_c_port_transforms(cstep, n, nz):
+    eps = O.eps_from_epssize(150, 2 * math.pi, n)
+    phi = O.ellipsoid_phi0(n, nz, eps, (1.6, 1.6, 0.8))
+    c = cstep.CStep(n, nz, eps)
+    cal = O.Calc(n, nz, 2 * math.pi)
+    s = c.r2c(phi)
+    assert np.abs(s - cal.r2c_3d_f(phi)).max() < 1e-15
+    assert np.abs(c.c2r(s) - phi).max() < 1e-14
+    c.close()
+
+
+@pytest.mark.parametrize("method,fixed,nsteps", [("euler", 1e-7, 20), ("euler", 0.0, 10), ("etd2", 0.0, 20),
+                                                  ("etd2", 1e-6, 5)])
+def test_c_port_loops(cstep, method, fixed, nsteps):
+    n = 24
+    eps = O.eps_from_epssize(150, 2 * math.pi, n)
+    phi = O.ellipsoid_phi0(n, n, eps, (1.6, 1.6, 0.8))
+    ts = 1e-7 if method == "euler" else 1e-6
+    b = O.Belastic(O.Params(nx=n, nz=n, eps=eps, time_step=ts, fixed_time_step=fixed), phi)
+    why = b.run_static(nsteps) if method == "euler" else b.run_static_fEIF(nsteps, method)
+    c = cstep.CStep(n, n, eps)
+    c.set_phi(phi)
+    assert c.run(method, nsteps, ts, fixed) == why
+    s = c.scalars()
+    assert (s["steps"], s["rejects"]) == (b.steps, b.rejects)
+    assert np.abs(c.get_phi() - b.pd.d).max() < 1e-12
+    assert s["E"] == pytest.approx(b.getstaticenergy(b.pd), rel=1e-12)
+    c.close()
+
+
+# ---------------------------------------------------------------- golden pins
+def _manifest():
+    if not os.path.exists(MANIFEST):
+        pytest.skip("golden vectors not generated")
+    return json.load(open(MANIFEST))
+
+
+FIELD_CASES = ["f16", "f24", "f32x16"]
+
+
+@pytest.mark.parametrize("name", FIELD_CASES)
+def test_oracle_fields_match_reference(name):
+    man = _manifest()
+    case = man["cases"][name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    sc = case["scalars"]
+    nx, nz = case["nx"], case["nz"]
+    eps = O.eps_from_epssize(case["epssize"], 2 * math.pi, nx)
+    assert eps == pytest.approx(sc["eps"], rel=1e-15)
+    dt = case["dt"]
+    b = O.Belastic(O.Params(nx=nx, nz=nz, eps=eps, time_step=dt, fixed_time_step=dt), g["phi0"])
+    b.set_alpha_beta_from_t0()
+    pd = b.pd
+
+    def close(a, ref, tol=1e-11):
+        err = np.abs(a - ref).max() / max(np.abs(ref).max(), 1e-300)
+        assert err < tol, err
+
+    close(pd.fd(), g["fd"])
+    close(pd.lap(), g["lap"])
+    close(pd.f(), g["f"])
+    close(pd.g0(), g["g0"])
+    close(pd.nld(), g["nld"])
+    dx, dy, dz = pd.gradient()
+    close(dx, g["dx"]); close(dy, g["dy"]); close(dz, g["dz"])
+    close(pd.s(), g["s"])
+    close(b.get_sum_fgqterm(pd), g["rhs_euler"])
+    close(b.get_nld_term(pd), g["nld_hat"])
+    b.init_fEIF()
+    close(b.Het, g["Het"], 1e-15)
+    for k in ("V", "S", "E_el", "E"):
+        ref = sc[k]
+        got = {"V": pd.vol(), "S": pd.surface(), "E_el": pd.elastic_eng(), "E": b.getstaticenergy(pd)}[k]
+        assert got == pytest.approx(ref, rel=1e-12), k
+    assert pd.LSerror(b.get_sum_fgqterm(pd)) == pytest.approx(sc["LSerror"], rel=1e-10)
+    # one step of each method from phi0
+    phi0 = g["phi0"].copy()
+    R = b.get_sum_fgqterm(pd)
+    b.euler_update(R)
+    close(b.pd.d, g["euler1"], 1e-13)
+    b.pd.d = phi0.copy(); b.pd.update_d()
+    b.ETD2RK()
+    close(b.pd.d, g["etd2_1"], 1e-12)
+    b.pd.d = phi0.copy(); b.pd.update_d()
+    b.ETD4RK()
+    # the reference's closed-form ETD-RK4 weights carry ~1e-16/|hL|^3 relative
+    # noise (Calc.cu:558-567); at these grids |hL(0)| ~ 1e-5 so only the
+    # bulk of the field is comparable
+    close(b.pd.d, g["etd4_1"], 1e-6)
+
+
+RUN_CASES = [("euler32", 1e-12), ("euler32_adapt", 1e-12), ("etd2_32", 1e-10), ("etd2_48", 1e-10)]
+
+
+@pytest.mark.parametrize("name,tol", RUN_CASES)
+def test_oracle_trajectories_match_reference(name, tol):
+    man = _manifest()
+    case = man["cases"][name]
+    snaps = np.load(os.path.join(GOLDEN, name + ".npz"))
+    nx, nz = case["nx"], case["nz"]
+    eps = O.eps_from_epssize(case["epssize"], 2 * math.pi, nx)
+    b = O.Belastic(O.Params(nx=nx, nz=nz, eps=eps, time_step=case["time_step"],
+                            fixed_time_step=case["fixed"], M1=case["M"], M2=case["M"]), snaps["phi_000000"])
+    steps = case["steps"]
+    last = steps[-1]
+    if case["method"] == "euler":
+        why = b.run_static(last["step"])
+    else:
+        why = b.run_static_fEIF(last["step"], case["method"])
+    assert why == "max_steps" and case["end"]["end"] == "max_steps"
+    assert b.rejects == case["end"]["rejects"]
+    assert b.time_step == pytest.approx(last["dt"], rel=1e-15)
+    key = "phi_%06d" % last["step"]
+    err = np.abs(b.pd.d - snaps[key]).max()
+    assert err < tol, err
+    assert b.getstaticenergy(b.pd) == pytest.approx(last["E"], rel=1e-11)
