@@ -73,6 +73,7 @@ struct Params {
     double invN;
     double grow_factor, dt_cap, cap_probe, dt_min;
     double tmax;        // Euler loop time limit (belastic.cpp:407)
+    double rel_tol;     // > 0: stop once an accepted step changes E by < rel_tol |E|
 };
 
 // exit reasons kept in Ctrl::status (mirrors the public CB_* codes)

@@ -145,6 +145,8 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     c->t += c->dt;
     c->steps++;
     if (c->steps >= c->target) { c->done = 1; c->status = ST_TARGET; }
+    // relaxation criterion |dE / E| < rel_tol (no counterpart in the reference loops)
+    if (!raw && p.rel_tol > 0.0 && fabs(E1 - E0) < p.rel_tol * fabs(E1)) { c->done = 1; c->status = ST_CONVERGED; }
     if (!raw && p.adaptive && c->steps % p.grow_every == 0)
         c->dt = (c->dt * p.cap_probe < p.dt_cap) ? c->dt * p.grow_factor : p.dt_cap;
 }

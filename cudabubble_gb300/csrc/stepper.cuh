@@ -1,0 +1,794 @@
+// Host side of the GB300 stepper: one instance (vesicle) per handle, the
+// per-attempt kernel sequence captured once into a CUDA graph, and the
+// reference time loops driven from device-side accept/reject state.  The C
+// ABI of include/cbstep.h is in stepper.cu; batched and served pools of
+// instances are in pool.cu.
+//
+// Attempt sequences (every kernel reads its instance's Ctrl block, so the
+// graph is replayed unchanged while dt, the state index and the accept flag
+// live on the device):
+//   ETD-RK2 (belastic.cpp:491-517)
+//     xy NONLIN(state) -> z ETD2_S1 -> xy REDUCE_S(work) -> xy NONLIN(work)
+//     -> z ETD2_S2 -> xy REDUCE_FULL(cand) -> decide -> coef
+//   ETD-RK4 (belastic.cpp:519-552): four stages of the same shape
+//   Euler   (belastic.cpp:52-64, 382): xy NONLIN(state) -> z EULER
+//     -> xy REDUCE_FULL(cand) -> decide
+// The stage-1 nonlinear spectrum does not depend on dt, so a rejected attempt
+// reuses it (the xy NONLIN on the state is skipped while ctrl->fresh == 0).
+#pragma once
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "cb_inst.h"
+#include "cb_kargs.h"
+#include "cbstep.h"
+#include "launch.h"
+
+namespace cb {
+
+inline thread_local std::string g_err;
+
+inline int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CB_CK(x)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (x);                                                                       \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(CB_ECUDA, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+inline constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+// ------------------------------------------------------------ twiddles
+// W_n^m = exp(-2 pi i m / n), evaluated in long double and rounded once.
+inline std::mutex g_tw_mu;
+inline std::map<std::tuple<int, int, int, int>, void*> g_tw;
+
+template <class T> inline void* twiddle_table(int n, int xkind, cudaError_t* err) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    auto key = std::make_tuple(dev, (int)sizeof(T), n, xkind);
+    auto it = g_tw.find(key);
+    if (it != g_tw.end()) return it->second;
+    std::vector<T> v;
+    auto push = [&](int len) {
+        for (int m = 0; m < len; ++m) {
+            const long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)len;
+            v.push_back((T)cosl(a));
+            v.push_back((T)(-sinl(a)));
+        }
+    };
+    if (xkind) push(n / 2);  // half-length transform table, then the full one
+    push(n);
+    void* d = nullptr;
+    *err = cudaMalloc(&d, v.size() * sizeof(T));
+    if (*err != cudaSuccess) return nullptr;
+    *err = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (*err != cudaSuccess) return nullptr;
+    g_tw[key] = d;
+    return d;
+}
+
+// ------------------------------------------------------------ parameters
+inline double eps_rule(int epssize, double xlen, int nx) {  // fluidbase.cpp:68-108
+    const double h2 = 2 * xlen / 2.0 / nx;
+    switch (epssize) {
+        case 1: return 2.5 * (std::sqrt(2.) * xlen / 2.0 / nx);
+        case 2: return 2.5 * h2;
+        case 3: return 1.5 * h2;
+        case 4: return 1.25 * h2;
+        case 5: return 1.0 * h2;
+        case 6: return 0.7 * h2;
+        case 7: return 4.0 * h2;
+        case 8: return 2.5 * (std::sqrt(2.) * xlen / 2.0 / nx) * 1.22;
+        default: return epssize > 10 ? epssize / 100.0 * h2 : 2.0 * h2;
+    }
+}
+
+struct Eff {
+    Params p;
+    double dt0;
+    int accurate;
+    int precision;
+};
+
+inline int make_params(const cb_params& u, Eff& e) {
+    Params& p = e.p;
+    memset(&p, 0, sizeof p);
+    if (u.nx <= 0 || u.nz <= 0 || (u.nx & 1))
+        return fail(CB_EINVAL, "grid %dx%dx%d: nx must be even and positive (Calc.cu:52-55)", u.nx, u.nx, u.nz);
+    if (u.method < CB_EULER || u.method > CB_ETD4) return fail(CB_EINVAL, "unknown method %d", u.method);
+    if (u.precision != CB_FP64 && u.precision != CB_FP32) return fail(CB_EINVAL, "unknown precision %d", u.precision);
+    p.nx = u.nx;
+    p.ny = u.nx;  // Calc.cu:45-46
+    p.nz = u.nz;
+    p.nc = u.nx / 2 + 1;
+    p.N = (long long)p.nx * p.ny * p.nz;
+    p.invN = 1.0 / (double)p.N;
+    const double xlen = (u.lenx > 0 ? u.lenx : 1.0) * kTwoPi;
+    p.cx = (kTwoPi / xlen) * (kTwoPi / xlen);
+    p.L3 = xlen * xlen * xlen;
+    p.eps = u.eps > 0 ? u.eps : eps_rule(u.epssize, xlen, u.nx);
+    p.eta = u.eta;
+    p.ga = u.ga;
+    p.M1 = u.M1;
+    p.M2 = u.M2;
+    p.method = u.method;
+    p.adaptive = u.fixed_time_step <= 0;
+    p.corr = (!p.adaptive && u.method != CB_EULER && (u.M1 != 0 || u.M2 != 0)) ? 1 : 0;
+    p.etd4_ref = u.etd4_textbook ? 0 : 1;
+    p.kmax = (p.nx / 2) * (p.nx / 2) + (p.ny / 2) * (p.ny / 2) + (p.nz / 2) * (p.nz / 2);
+    const bool euler = u.method == CB_EULER;
+    p.grow_every = u.grow_every > 0 ? u.grow_every : 4;
+    p.grow_factor = u.grow_factor > 0 ? u.grow_factor : (euler ? 1.4 : 2.0);
+    p.dt_cap = u.dt_cap > 0 ? u.dt_cap : (euler ? 1e300 : 1e-3);
+    p.cap_probe = u.cap_probe > 0 ? u.cap_probe : (euler ? 0.0 : 1.4);
+    p.dt_min = 1e-23;
+    p.tmax = u.tmax >= 0 ? u.tmax : 4.0;
+    p.rel_tol = u.rel_tol > 0 ? u.rel_tol : 0.0;
+    const double ts = u.time_step > 0 ? u.time_step : 1e-6;  // fluidbase.cpp:112
+    e.dt0 = p.adaptive ? ts : std::min(u.fixed_time_step, ts);  // belastic.cpp:599-602
+    e.precision = u.precision;
+    e.accurate = u.accurate_coefficients >= 0 ? u.accurate_coefficients : (u.precision == CB_FP32 ? 1 : 0);
+    return CB_OK;
+}
+
+// ------------------------------------------------------------ instance
+struct Handle {
+    virtual ~Handle() {}
+    virtual int init(const cb_params& u) = 0;
+    virtual int set_phi(const double* phi, bool dev) = 0;
+    virtual int get_phi(double* phi, bool dev) = 0;
+    virtual int scalars(cb_scalars* s) = 0;
+    virtual int raw_step(int method) = 0;
+    virtual int run(int nsteps, cb_run_stats* st) = 0;
+    virtual int field(int which, double* out, bool dev) = 0;
+    virtual int set_dt(double dt) = 0;
+    virtual int sync() = 0;
+    virtual long long bytes() const = 0;
+    virtual int run_timed(int nsteps, long long flush_bytes, double* ms, int* attempts) = 0;
+    virtual int profile(int nattempts, long long flush_bytes, double* ms, int* cnt) = 0;
+};
+
+// kernel kinds reported by cb_profile_kernels
+enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, K_DECIDE = 4, K_NKIND = 5 };
+
+// One attempt of the method's loop for `ninst` instances that share grid and
+// method (an instance table on the device), on stream s.  With prof set, an
+// event pair brackets every launch and is appended as (kind, start, end).
+template <class T>
+inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, int ninst, int ntiles, int accurate,
+                                 bool raw, cudaStream_t s,
+                                 std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
+    cudaError_t r = cudaSuccess;
+    auto timed = [&](int kind, auto&& fn) {
+        if (r != cudaSuccess) return;
+        if (!prof) { r = fn(); return; }
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+        r = fn();
+        cudaEventRecord(b, s);
+        prof->emplace_back(kind, a, b);
+    };
+    auto X = [&](int m, int role, int skip = 0) {
+        const int kind = m == XY_NONLIN ? K_XY_NONLIN : (m == XY_REDUCE_S ? K_XY_REDUCE_S : K_XY_REDUCE_FULL);
+        timed(kind, [&]() {
+            XYArgs a;
+            memset(&a, 0, sizeof a);
+            a.mode = m;
+            a.role = role;
+            a.skip_if_stale = skip;
+            return Launch<T>::xy(nx, d, ninst, nz, a, s);
+        });
+    };
+    auto Z = [&](int m, int role) {
+        timed(K_Z_STAGE, [&]() {
+            ZArgs a;
+            memset(&a, 0, sizeof a);
+            a.mode = m;
+            a.role = role;
+            return Launch<T>::z(nz, d, ninst, ntiles, a, s);
+        });
+    };
+    switch (method) {
+        case M_ETD2:
+            X(XY_NONLIN, R_STATE, 1);
+            Z(Z_ETD2_S1, R_WORK);
+            X(XY_REDUCE_S, R_WORK);
+            X(XY_NONLIN, R_WORK);
+            Z(Z_ETD2_S2, R_CAND);
+            X(XY_REDUCE_FULL, R_CAND);
+            break;
+        case M_ETD4:
+            X(XY_NONLIN, R_STATE, 1);
+            Z(Z_ETD4_S1, R_WORK);
+            X(XY_REDUCE_S, R_WORK);
+            X(XY_NONLIN, R_WORK);
+            Z(Z_ETD4_S2, R_WORK);
+            X(XY_REDUCE_S, R_WORK);
+            X(XY_NONLIN, R_WORK);
+            Z(Z_ETD4_S3, R_WORK);
+            X(XY_REDUCE_S, R_WORK);
+            X(XY_NONLIN, R_WORK);
+            Z(Z_ETD4_S4, R_CAND);
+            X(XY_REDUCE_FULL, R_CAND);
+            break;
+        default:
+            X(XY_NONLIN, R_STATE, 1);
+            Z(Z_EULER, R_CAND);
+            X(XY_REDUCE_FULL, R_CAND);
+            break;
+    }
+    timed(K_DECIDE, [&]() {
+        cudaError_t q = Launch<T>::decide(d, ninst, raw ? 1 : 0, s);
+        return q == cudaSuccess ? Launch<T>::coef(d, ninst, accurate, s) : q;
+    });
+    return r;
+}
+
+template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* layout = nullptr) {
+    const size_t ns = (size_t)p.nz * p.ny * p.nc * sizeof(T) * 2;
+    const int ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const int nfields = 12 + (p.method == M_ETD4 ? 2 : 0);
+    size_t off = 0;
+    if (layout) layout[0] = off;
+    off += al(ns) * nfields;
+    if (layout) layout[1] = off;
+    off += al((size_t)(p.kmax + 1) * 8 * sizeof(T));
+    if (layout) layout[2] = off;
+    off += al((size_t)p.nz * 4 * sizeof(double));
+    if (layout) layout[3] = off;
+    off += al((size_t)ntiles * 2 * sizeof(double));
+    if (layout) layout[4] = off;
+    off += al(sizeof(Ctrl));
+    if (layout) layout[5] = off;
+    off += al(sizeof(InstT<T>));
+    return off;
+}
+
+template <class T> class Stepper final : public Handle {
+   public:
+    ~Stepper() override {
+        if (st) cudaStreamSynchronize(st);
+        if (g_loop) cudaGraphExecDestroy(g_loop);
+        if (g_raw) cudaGraphExecDestroy(g_raw);
+        cudaFree(arena);
+        cudaFree(scratch);
+        cudaFree(cbuf);
+        cudaFree(flush_buf);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int init(const cb_params& u) override {
+        up = u;
+        int rc = make_params(u, e);
+        if (rc) return rc;
+        p = e.p;
+        if (!Launch<T>::xy_supported(p.nx) || !Launch<T>::z_supported(p.nz))
+            return fail(CB_EUNSUPPORTED, "grid %dx%dx%d not built for %s", p.nx, p.ny, p.nz,
+                        sizeof(T) == 4 ? "FP32" : "FP64");
+        ns = (size_t)p.nz * p.ny * p.nc;
+        ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
+        size_t lay[6];
+        arena_bytes = instance_arena_bytes<T>(p, lay);
+        CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CB_ENOMEM, "cudaMalloc of %zu bytes failed", arena_bytes);
+        }
+        CB_CK(cudaMemsetAsync(arena, 0, arena_bytes, st));
+        char* base = (char*)arena;
+        const size_t fb = ((ns * sizeof(T) * 2) + 255) & ~(size_t)255;
+        void** f[14] = {&h.spec[0], &h.spec[1], &h.ahat, &h.Nu, &h.P[0][0], &h.P[0][1], &h.P[1][0], &h.P[1][1],
+                        &h.P[2][0], &h.P[2][1], &h.A, &h.B, &h.Na, &h.Nb};
+        const int nfields = 12 + (p.method == M_ETD4 ? 2 : 0);
+        for (int i = 0; i < nfields; ++i) *f[i] = base + lay[0] + i * fb;
+        h.coef = reinterpret_cast<T*>(base + lay[1]);
+        h.part_xy = reinterpret_cast<double*>(base + lay[2]);
+        h.part_z = reinterpret_cast<double*>(base + lay[3]);
+        h.ctrl = reinterpret_cast<Ctrl*>(base + lay[4]);
+        d = reinterpret_cast<InstT<T>*>(base + lay[5]);
+        cudaError_t err = cudaSuccess;
+        h.twx = twiddle_table<T>(p.nx, 1, &err);
+        if (!h.twx) return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(err));
+        h.twy = twiddle_table<T>(p.ny, 0, &err);
+        if (!h.twy) return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(err));
+        h.twz = twiddle_table<T>(p.nz, 0, &err);
+        if (!h.twz) return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(err));
+        h.p = p;
+        CB_CK(cudaMemcpyAsync(d, &h, sizeof h, cudaMemcpyHostToDevice, st));
+        memset(&hc, 0, sizeof hc);
+        reset_ctrl();
+        CB_CK(push());
+        return CB_OK;
+    }
+
+    long long bytes() const override { return (long long)arena_bytes; }
+
+    // phi staging buffer: the two work partials are contiguous in the arena and
+    // hold at least N doubles; A is the transform intermediate.  Both are
+    // free between attempts, so set/get_phi allocate nothing.
+    double* stage() const { return reinterpret_cast<double*>(h.P[2][0]); }
+
+    int set_phi(const double* phi, bool dev) override {
+        const double* src = phi;
+        if (!dev) {
+            CB_CK(cudaMemcpyAsync(stage(), phi, (size_t)p.N * sizeof(double), cudaMemcpyHostToDevice, st));
+            src = stage();
+        }
+        reset_ctrl();
+        CB_CK(push());
+        CB_CK(fwd3d(src, h.spec[0], h.A));
+        CB_CK(zpass(Z_INV_STATE, R_STATE));
+        CB_CK(xypass(XY_REDUCE_FULL, R_STATE));
+        CB_CK(pull());
+        // alpha/beta from t = 0 when beta <= 0 (fluidbase.cpp:143, belastic.cpp:588-591)
+        if (!(up.beta > 0.0)) {
+            hc.alpha = hc.sc[R_STATE].V;
+            hc.beta = hc.sc[R_STATE].S;
+        } else {
+            hc.alpha = up.alpha;
+            hc.beta = up.beta;
+        }
+        hc.alpha0 = hc.alpha;
+        hc.beta0 = hc.beta;
+        Scal& s = hc.sc[R_STATE];
+        const double ve = s.V - hc.alpha, se = s.S - hc.beta;
+        s.E = p.eta * s.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
+        hc.E_state = hc.E_init = s.E;
+        CB_CK(push());
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        have_state = true;
+        grown0 = false;
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    int get_phi(double* out, bool dev) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        CB_CK(pull());
+        double* dst = dev ? out : stage();
+        CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A));
+        if (!dev) CB_CK(cudaMemcpyAsync(out, stage(), (size_t)p.N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    int scalars(cb_scalars* s) override {
+        CB_CK(pull());
+        const Scal& sc = hc.sc[R_STATE];
+        s->V = sc.V;
+        s->S = sc.S;
+        s->E_el = sc.E_el;
+        s->E = hc.E_state;
+        s->alpha = hc.alpha;
+        s->beta = hc.beta;
+        s->lamb1 = p.M1 * (sc.V - hc.alpha);
+        s->lamb2 = p.M2 * (sc.S - hc.beta);
+        s->dt = hc.dt;
+        s->t = hc.t;
+        s->lserror = sc.lsq * p.L3;
+        s->steps = hc.steps;
+        s->attempts = hc.attempts;
+        s->rejects = hc.rejects;
+        s->status = last_status;
+        return CB_OK;
+    }
+
+    int set_dt(double dt) override {
+        if (!(dt > 0)) return fail(CB_EINVAL, "dt must be positive");
+        CB_CK(pull());
+        hc.dt = dt;
+        CB_CK(push());
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    int sync() override {
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    int raw_step(int method) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        if (method != p.method) return fail(CB_EINVAL, "handle was created for method %d, not %d", p.method, method);
+        CB_CK(pull());
+        hc.target = INT_MAX;
+        hc.done = 0;
+        CB_CK(push());
+        if (!g_raw) {
+            int rc = capture(true, &g_raw);
+            if (rc) return rc;
+        }
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaGraphLaunch(g_raw, st));
+        CB_CK(pull());
+        last_status = hc.status;
+        if (hc.nonfinite) return fail(CB_ENONFINITE, "state is no longer finite");
+        return CB_OK;
+    }
+
+    int run(int nsteps, cb_run_stats* stt) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        if (nsteps < 0) return fail(CB_EINVAL, "nsteps < 0");
+        CB_CK(pull());
+        if (p.adaptive && !grown0 && hc.steps % p.grow_every == 0) {  // first step's growth
+            hc.dt = (hc.dt * p.cap_probe < p.dt_cap) ? hc.dt * p.grow_factor : p.dt_cap;
+        }
+        grown0 = true;
+        const int steps0 = hc.steps, att0 = hc.attempts;
+        hc.target = hc.steps + nsteps;
+        hc.done = nsteps == 0 ? 1 : 0;
+        hc.status = nsteps == 0 ? ST_TARGET : ST_RUNNING;
+        CB_CK(push());
+        if (!g_loop) {
+            int rc = capture(false, &g_loop);
+            if (rc) return rc;
+        }
+        cudaEvent_t e0, e1;
+        CB_CK(cudaEventCreate(&e0));
+        CB_CK(cudaEventCreate(&e1));
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaEventRecord(e0, st));
+        int launches = 0;
+        const long long limit = 70LL * (nsteps + 1) * (p.corr ? 2 : 1) + 1000;
+        while (!hc.done) {
+            const int remaining = hc.target - hc.steps;
+            int chunk = remaining * (p.corr ? 2 : 1) + remaining / 8 + 1;
+            chunk = std::max(1, std::min(chunk, 512));
+            for (int i = 0; i < chunk; ++i) CB_CK(cudaGraphLaunch(g_loop, st));
+            launches += chunk;
+            CB_CK(pull());
+            if (launches > limit) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return fail(CB_ENOTCONVERGED, "no progress after %d attempts", launches);
+            }
+        }
+        CB_CK(cudaEventRecord(e1, st));
+        CB_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        last_status = hc.status;
+        if (stt) {
+            stt->steps = hc.steps - steps0;
+            stt->attempts = hc.attempts - att0;
+            stt->status = hc.status;
+            stt->graph_launches = launches;
+            stt->device_ms = ms;
+        }
+        // leave the instance live for getters and further runs
+        hc.done = 0;
+        CB_CK(push());
+        CB_CK(cudaStreamSynchronize(st));
+        switch (last_status) {
+            case ST_NONFINITE: return fail(CB_ENONFINITE, "state blew up (non-finite energy)");
+            case ST_DT_UNDERFLOW: return fail(CB_EDTUNDERFLOW, "adaptive dt fell below %g", p.dt_min);
+            default: return CB_OK;
+        }
+    }
+
+    int field(int which, double* out, bool dev) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        int rc = ensure_scratch();
+        if (rc) return rc;
+        CB_CK(pull());
+        const size_t N = (size_t)p.N;
+        const bool cplx_out = which == CB_FIELD_FD || which == CB_FIELD_NLD_HAT;
+        const size_t out_doubles = cplx_out ? 2 * ns : N;
+        double* dst = dev ? out : rbuf[5];
+        if (cplx_out && !dev) {
+            if (!cbuf) CB_CK(cudaMalloc(&cbuf, 2 * ns * sizeof(double)));
+            dst = cbuf;
+        }
+        const void* phat = h.spec[hc.spec_state];
+        double* phi = rbuf[0];
+        auto need_phi = [&]() { return inv3d(phat, SM_NONE, phi); };
+        const double eps = p.eps;
+        switch (which) {
+            case CB_FIELD_PHI: CB_CK(inv3d(phat, SM_NONE, dst)); break;
+            case CB_FIELD_FD: CB_CK(Launch<T>::to_double(phat, dst, ns, st)); break;
+            case CB_FIELD_LAP: CB_CK(inv3d(phat, SM_LAP, dst)); break;
+            case CB_FIELD_DX: CB_CK(inv3d(phat, SM_DX, dst)); break;
+            case CB_FIELD_DY: CB_CK(inv3d(phat, SM_DY, dst)); break;
+            case CB_FIELD_DZ: CB_CK(inv3d(phat, SM_DZ, dst)); break;
+            case CB_FIELD_F:
+            case CB_FIELD_G0:
+            case CB_FIELD_NLD: {
+                CB_CK(need_phi());
+                CB_CK(inv3d(phat, SM_LAP, rbuf[1]));
+                double* f = which == CB_FIELD_F ? dst : rbuf[2];
+                CB_CK(launch_pointwise(0, N, f, phi, rbuf[1], nullptr, nullptr, eps, 0, 0, 0, st));
+                if (which == CB_FIELD_G0) {  // Calc.cu:171-188: g0 = -lap f + (3 phi^2 - 1) f / eps^2
+                    CB_CK(fwd3d(f, tmpS));
+                    CB_CK(inv3d(tmpS, SM_LAP, rbuf[3]));
+                    CB_CK(launch_pointwise(1, N, dst, phi, f, rbuf[3], nullptr, eps, 0, 0, 0, st));
+                } else if (which == CB_FIELD_NLD) {  // Calc.cu:265-297
+                    CB_CK(launch_pointwise(2, N, rbuf[3], phi, nullptr, nullptr, nullptr, eps, 0, 0, 0, st));
+                    CB_CK(fwd3d(rbuf[3], tmpS));
+                    CB_CK(inv3d(tmpS, SM_LAP, rbuf[4]));
+                    CB_CK(launch_pointwise(3, N, dst, phi, f, rbuf[3], rbuf[4], eps, 0, 0, 0, st));
+                }
+                break;
+            }
+            case CB_FIELD_S: {  // Calc.cu:358-374
+                CB_CK(need_phi());
+                CB_CK(inv3d(phat, SM_DX, rbuf[1]));
+                CB_CK(inv3d(phat, SM_DY, rbuf[2]));
+                CB_CK(inv3d(phat, SM_DZ, rbuf[3]));
+                CB_CK(launch_pointwise(4, N, dst, phi, rbuf[1], rbuf[2], rbuf[3], eps, 0, 0, 0, st));
+                break;
+            }
+            case CB_FIELD_NLD_HAT:
+            case CB_FIELD_RHS: {
+                // the hot-path kernels themselves: xy NONLIN on the state, then the
+                // stage-1 z pass leaves N_u (ETD) or R-hat (Euler) in the Nu buffer
+                const bool etd = p.method != M_EULER;
+                if ((which == CB_FIELD_NLD_HAT) != etd)
+                    return fail(CB_EINVAL, "field %d needs a %s handle", which, etd ? "Euler" : "ETD");
+                hc.fresh = 1;
+                hc.done = 0;
+                CB_CK(push());
+                CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+                CB_CK(xypass(XY_NONLIN, R_STATE));
+                CB_CK(zpass(etd ? (p.method == M_ETD2 ? Z_ETD2_S1 : Z_ETD4_S1) : Z_EULER, etd ? R_WORK : R_CAND));
+                if (etd) CB_CK(Launch<T>::to_double(h.Nu, dst, ns, st));
+                else CB_CK(inv3d(h.Nu, SM_NONE, dst));
+                break;
+            }
+            default: return fail(CB_EINVAL, "unknown field %d", which);
+        }
+        if (!dev) CB_CK(cudaMemcpyAsync(out, dst, out_doubles * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    // Same loop as run(), one attempt at a time, each bracketed by CUDA events
+    // on the handle's stream; an optional L2 flush (memset of flush_bytes)
+    // runs between attempts, outside the timed events.
+    int run_timed(int nsteps, long long flush_bytes, double* ms_out, int* att_out) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        CB_CK(pull());
+        if (p.adaptive && !grown0 && hc.steps % p.grow_every == 0)
+            hc.dt = (hc.dt * p.cap_probe < p.dt_cap) ? hc.dt * p.grow_factor : p.dt_cap;
+        grown0 = true;
+        hc.target = hc.steps + nsteps;
+        hc.done = nsteps == 0 ? 1 : 0;
+        hc.status = ST_RUNNING;
+        CB_CK(push());
+        if (!g_loop) {
+            int rc = capture(false, &g_loop);
+            if (rc) return rc;
+        }
+        if (flush_bytes > 0 && flush_bytes != flush_size) {
+            cudaFree(flush_buf);
+            flush_buf = nullptr;
+            CB_CK(cudaMalloc(&flush_buf, (size_t)flush_bytes));
+            flush_size = flush_bytes;
+        }
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        cudaEvent_t e0, e1;
+        CB_CK(cudaEventCreate(&e0));
+        CB_CK(cudaEventCreate(&e1));
+        double total = 0.0;
+        int att = 0;
+        const long long limit = 70LL * (nsteps + 1) * (p.corr ? 2 : 1) + 1000;
+        while (!hc.done && att < limit) {
+            if (flush_bytes > 0) CB_CK(cudaMemsetAsync(flush_buf, att & 0xff, (size_t)flush_bytes, st));
+            CB_CK(cudaEventRecord(e0, st));
+            CB_CK(cudaGraphLaunch(g_loop, st));
+            CB_CK(cudaEventRecord(e1, st));
+            CB_CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CB_CK(cudaEventElapsedTime(&ms, e0, e1));
+            total += ms;
+            ++att;
+            CB_CK(pull());
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        last_status = hc.status;
+        hc.done = 0;
+        CB_CK(push());
+        CB_CK(cudaStreamSynchronize(st));
+        if (ms_out) *ms_out = total;
+        if (att_out) *att_out = att;
+        if (last_status == ST_NONFINITE) return fail(CB_ENONFINITE, "state blew up");
+        if (att >= limit) return fail(CB_ENOTCONVERGED, "no progress after %d attempts", att);
+        return CB_OK;
+    }
+
+    // nattempts loop attempts launched kernel by kernel (not from the graph),
+    // with an event pair around every launch; per kind, the summed device time
+    // and launch count.  Kernels that exit early (skipped stage 1) still count.
+    int profile(int nattempts, long long flush_bytes, double* ms, int* cnt) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        for (int k = 0; k < K_NKIND; ++k) { ms[k] = 0.0; cnt[k] = 0; }
+        CB_CK(pull());
+        hc.target = INT_MAX;
+        hc.done = 0;
+        CB_CK(push());
+        if (flush_bytes > 0 && flush_bytes != flush_size) {
+            cudaFree(flush_buf);
+            flush_buf = nullptr;
+            CB_CK(cudaMalloc(&flush_buf, (size_t)flush_bytes));
+            flush_size = flush_bytes;
+        }
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        for (int a = 0; a < nattempts; ++a) {
+            if (flush_bytes > 0) CB_CK(cudaMemsetAsync(flush_buf, a & 0xff, (size_t)flush_bytes, st));
+            std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>> prof;
+            int rc = enqueue_attempt(false, &prof);
+            if (rc) return rc;
+            CB_CK(cudaStreamSynchronize(st));
+            for (auto& t : prof) {
+                float m = 0.f;
+                cudaEventElapsedTime(&m, std::get<1>(t), std::get<2>(t));
+                ms[std::get<0>(t)] += m;
+                cnt[std::get<0>(t)] += 1;
+                cudaEventDestroy(std::get<1>(t));
+                cudaEventDestroy(std::get<2>(t));
+            }
+        }
+        CB_CK(pull());
+        hc.done = 0;
+        CB_CK(push());
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+   private:
+    void reset_ctrl() {
+        Ctrl c;
+        memset(&c, 0, sizeof c);
+        c.dt = e.dt0;
+        c.alpha = up.alpha;
+        c.beta = up.beta;
+        c.fresh = 1;
+        c.target = INT_MAX;
+        hc = c;
+        last_status = ST_RUNNING;
+    }
+    cudaError_t push() { return cudaMemcpyAsync(h.ctrl, &hc, sizeof hc, cudaMemcpyHostToDevice, st); }
+    cudaError_t pull() {
+        cudaError_t r = cudaMemcpyAsync(&hc, h.ctrl, sizeof hc, cudaMemcpyDeviceToHost, st);
+        if (r != cudaSuccess) return r;
+        return cudaStreamSynchronize(st);
+    }
+    cudaError_t xypass(int mode, int role, int skip = 0) {
+        XYArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = mode;
+        a.role = role;
+        a.skip_if_stale = skip;
+        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+    }
+    cudaError_t zpass(int mode, int role) {
+        ZArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = mode;
+        a.role = role;
+        return Launch<T>::z(p.nz, d, 1, ntiles, a, st);
+    }
+    // real double field -> spectrum (x 1/N), through the partial buffer `part`
+    cudaError_t fwd3d(const double* src, void* spec, void* part = nullptr) {
+        if (!part) part = tmpP;
+        XYArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = XY_FWD_PLAIN;
+        a.rin = src;
+        a.cout = part;
+        cudaError_t r = Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+        if (r != cudaSuccess) return r;
+        ZArgs z;
+        memset(&z, 0, sizeof z);
+        z.mode = Z_FWD_PLAIN;
+        z.cin = part;
+        z.cout = spec;
+        return Launch<T>::z(p.nz, d, 1, ntiles, z, st);
+    }
+    // spectrum (x multiplier) -> real double field, through `part`
+    cudaError_t inv3d(const void* spec, int mul, double* dst, void* part = nullptr) {
+        if (!part) part = tmpP;
+        ZArgs z;
+        memset(&z, 0, sizeof z);
+        z.mode = Z_INV_PLAIN;
+        z.mul = mul;
+        z.cin = spec;
+        z.cout = part;
+        cudaError_t r = Launch<T>::z(p.nz, d, 1, ntiles, z, st);
+        if (r != cudaSuccess) return r;
+        XYArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = XY_INV_PLAIN;
+        a.cin = part;
+        a.rout = dst;
+        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+    }
+    int ensure_scratch() {
+        if (scratch) return CB_OK;
+        const size_t N = (size_t)p.N;
+        const size_t cb = ((ns * sizeof(T) * 2) + 255) & ~(size_t)255;
+        const size_t rb = ((N * sizeof(double)) + 255) & ~(size_t)255;
+        if (cudaMalloc(&scratch, 2 * cb + 6 * rb) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CB_ENOMEM, "scratch allocation failed");
+        }
+        tmpP = scratch;
+        tmpS = (char*)scratch + cb;
+        for (int i = 0; i < 6; ++i) rbuf[i] = reinterpret_cast<double*>((char*)scratch + 2 * cb + i * rb);
+        return CB_OK;
+    }
+    // prof != nullptr: record an event pair around every launch (profiling; not captured)
+    int enqueue_attempt(bool raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
+        cudaError_t r = enqueue_group<T>(p.method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw, st, prof);
+        if (r != cudaSuccess) return fail(CB_ECUDA, "enqueue attempt: %s", cudaGetErrorString(r));
+        return CB_OK;
+    }
+    int capture(bool raw, cudaGraphExec_t* out) {
+        cudaGraph_t g = nullptr;
+        CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_attempt(raw);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CB_CK(ce);
+        cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        CB_CK(ie);
+        return CB_OK;
+    }
+
+    cb_params up{};
+    Eff e{};
+    Params p{};
+    InstT<T> h{};
+    InstT<T>* d = nullptr;
+    Ctrl hc{};
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    void* scratch = nullptr;
+    void* tmpP = nullptr;
+    void* tmpS = nullptr;
+    double* rbuf[6] = {};
+    double* cbuf = nullptr;
+    size_t ns = 0;
+    int ntiles = 0;
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t g_loop = nullptr, g_raw = nullptr;
+    void* flush_buf = nullptr;
+    long long flush_size = 0;
+    bool have_state = false, grown0 = false;
+    int last_status = ST_RUNNING;
+};
+
+}  // namespace cb
+

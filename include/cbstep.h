@@ -90,6 +90,8 @@ typedef struct cb_params {
     double cap_probe;        /* 0: method default (1.4 ETD) */
     int etd4_textbook;       /* 1: Cox-Matthews combine with N_u; 0: the reference's N_a (belastic.cpp:550) */
     int accurate_coefficients; /* -1: default (FP32 form: phi-function series; FP64 form: reference closed forms) */
+    double rel_tol;          /* > 0: cb_run stops (CB_DONE_CONVERGED) once an accepted step changes
+                                E by less than rel_tol |E|; not in the reference loops */
 } cb_params;
 
 typedef struct cb_scalars {

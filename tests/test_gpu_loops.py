@@ -3,7 +3,10 @@ alpha/beta correction) against the FP64 oracle's restatement of
 belastic.cpp:286-470 and :554-786, through the C ABI.
 
 FP64 form: the accepted-step count, rejection count and final dt must match
-exactly and max|phi - phi_ref| <= 1e-10.
+exactly and max|phi - phi_ref| <= 1e-10.  ETD-RK4 cases use the phi-function
+coefficients on both sides: the reference's closed-form ETD-RK4 weights
+(Calc.cu:558-567) carry ~1e-16/|hL|^3 relative rounding noise, which at these
+small grids (|hL(0)| ~ 1e-4) makes two correct implementations disagree.
 """
 import math
 
@@ -37,14 +40,16 @@ def test_loop_fp64(cblib, case):
     name, method, n, es, ts, fixed, nsteps, seed = case
     phi0 = _phi0(n, es, seed)
     eps = O.eps_from_epssize(es, 2 * math.pi, n)
-    b = O.Belastic(O.Params(nx=n, nz=n, eps=eps, time_step=ts, fixed_time_step=fixed), phi0)
+    acc = method == "etd4"
+    b = O.Belastic(O.Params(nx=n, nz=n, eps=eps, time_step=ts, fixed_time_step=fixed, accurate_coefficients=acc),
+                   phi0)
     if method == "euler":
         why = b.run_static(nsteps)
     else:
         why = b.run_static_fEIF(nsteps, method)
     m = {"euler": capi.CB_EULER, "etd2": capi.CB_ETD2, "etd4": capi.CB_ETD4}[method]
     p = capi.default_params(nx=n, ny=n, nz=n, epssize=es, method=m, precision=capi.CB_FP64, time_step=ts,
-                            fixed_time_step=fixed)
+                            fixed_time_step=fixed, accurate_coefficients=int(acc))
     st = capi.Stepper(p)
     st.set_phi(phi0)
     r = st.run(nsteps)

@@ -165,13 +165,20 @@ def test_oracle_fields_match_reference(name):
     close(b.pd.d, g["etd2_1"], 1e-12)
     b.pd.d = phi0.copy(); b.pd.update_d()
     b.ETD4RK()
-    # the reference's closed-form ETD-RK4 weights carry ~1e-16/|hL|^3 relative
-    # noise (Calc.cu:558-567); at these grids |hL(0)| ~ 1e-5 so only the
-    # bulk of the field is comparable
-    close(b.pd.d, g["etd4_1"], 1e-6)
+    # The reference's closed-form ETD-RK4 weights (Calc.cu:558-567) sum O(1)
+    # terms to an O((hL)^3) result, so they carry ~1e-15/|hL|^3 relative
+    # rounding noise that depends on the exp() and FMA contraction of each
+    # implementation.  At these fixtures |hL(0)| is 6e-6 (16^3) and ~1e-4
+    # (24^3, 32x32x16); the tolerance follows that conditioning.
+    hl0 = abs(b.Het.flat[0] * dt)
+    close(b.pd.d, g["etd4_1"], 2e-5 if hl0 < 1e-5 else 1e-6)
 
 
-RUN_CASES = [("euler32", 1e-12), ("euler32_adapt", 1e-12), ("etd2_32", 1e-10), ("etd2_48", 1e-10)]
+RUN_CASES = [("euler32", 1e-12), ("euler32_adapt", 1e-12), ("etd2_32", 1e-10), ("etd2_48", 1e-10),
+             # workload config 1 at full size: 64^3 forward Euler, 1000 steps
+             ("c1_euler64", 1e-12),
+             # ETD-RK4: bounded by the reference's own coefficient noise (see above)
+             ("etd4_32", 2e-6), ("etd4_32_adapt", 3e-5)]
 
 
 @pytest.mark.parametrize("name,tol", RUN_CASES)
@@ -195,4 +202,4 @@ def test_oracle_trajectories_match_reference(name, tol):
     key = "phi_%06d" % last["step"]
     err = np.abs(b.pd.d - snaps[key]).max()
     assert err < tol, err
-    assert b.getstaticenergy(b.pd) == pytest.approx(last["E"], rel=1e-11)
+    assert b.getstaticenergy(b.pd) == pytest.approx(last["E"], rel=1e-11 if tol <= 1e-10 else 3e-4)
