@@ -148,15 +148,17 @@ def cpu_baseline(budget_s: float = 15.0):
 def algorithmic_bytes(n: int, fsize: int, att: int, rej: int):
     """Bytes each kernel kind must move over `att` attempts with `rej` retries
     (a retry skips the stage-1 nonlinear pass and reuses the stored N_u).
-    F = one half-spectrum complex field."""
+    F = one half-spectrum field of complex FP32 (8 B per mode); the stepped
+    state fields (phi-hat, candidate, a-hat) are double-float pairs, 2F."""
     F = n * n * (n // 2 + 1) * 2 * fsize
     return {
         "xy_nonlin": (2 * att - rej) * 4 * F,          # read P0, P2; write A, B
         "xy_reduce_s": att * 1 * F,                     # read P0
         "xy_reduce_full": att * 2 * F,                  # read P0, P2
-        "z_stage": att * 7 * F + (att - rej) * 7 * F + rej * 5 * F,
-        # S2: read A, B, a-hat, N_u; write phi', P0, P2.  S1 fresh: read A, B, phi; write N_u, a-hat, P0, P2
-        # S1 retry: read N_u, phi; write a-hat, P0, P2
+        # S2: read A, B, a-hat(2F), N_u; write phi'(2F), P0, P2          = 9F
+        # S1 fresh: read A, B, phi(2F); write N_u, a-hat(2F), P0, P2     = 9F
+        # S1 retry: read N_u, phi(2F); write a-hat(2F), P0, P2           = 7F
+        "z_stage": att * 9 * F + (att - rej) * 9 * F + rej * 7 * F,
     }, F
 
 

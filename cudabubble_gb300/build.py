@@ -20,7 +20,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libcbstep.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "stepper.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "stepper.cu", "pool.cu"]
 
 
 def nvcc() -> str:
@@ -44,8 +44,10 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, PKG):
         for f in os.listdir(d):
+            if not os.path.isfile(os.path.join(d, f)) or not f.endswith((".cu", ".cuh", ".h", "build.py")):
+                continue
             if os.path.getmtime(os.path.join(d, f)) > t:
                 return True
     return False

@@ -41,12 +41,30 @@ class cb_scalars(C.Structure):
     _fields_ = [("V", C.c_double), ("S", C.c_double), ("E_el", C.c_double), ("E", C.c_double),
                 ("lamb1", C.c_double), ("lamb2", C.c_double), ("alpha", C.c_double), ("beta", C.c_double),
                 ("dt", C.c_double), ("t", C.c_double), ("lserror", C.c_double), ("steps", C.c_int),
-                ("attempts", C.c_int), ("rejects", C.c_int), ("status", C.c_int)]
+                ("attempts", C.c_int), ("rejects", C.c_int), ("status", C.c_int), ("E_attempt", C.c_double)]
 
 
 class cb_run_stats(C.Structure):
     _fields_ = [("steps", C.c_int), ("attempts", C.c_int), ("status", C.c_int), ("graph_launches", C.c_int),
                 ("device_ms", C.c_double)]
+
+
+class cb_request(C.Structure):
+    _fields_ = [("params", cb_params), ("axes", C.c_double * 3), ("centre", C.c_double * 3),
+                ("axes2", C.c_double * 3), ("centre2", C.c_double * 3), ("arrival_s", C.c_double),
+                ("max_steps", C.c_int), ("pad", C.c_int)]
+
+
+class cb_result(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("admitted_s", C.c_double), ("finished_s", C.c_double),
+                ("latency_s", C.c_double), ("E", C.c_double), ("V", C.c_double), ("S", C.c_double),
+                ("steps", C.c_int), ("attempts", C.c_int), ("status", C.c_int), ("pad", C.c_int),
+                ("bytes", C.c_longlong)]
+
+
+class cb_serve_stats(C.Structure):
+    _fields_ = [("wall_s", C.c_double), ("point_steps", C.c_double), ("completed", C.c_int),
+                ("graph_launches", C.c_int), ("peak_bytes", C.c_longlong)]
 
 
 # every symbol include/cbstep.h declares, with its ctypes signature
@@ -73,6 +91,15 @@ SIGNATURES = {
     "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
     "cb_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
+    "cb_batch_create": (C.c_int, [_P(cb_params), C.c_int, _P(C.c_void_p)]),
+    "cb_batch_destroy": (C.c_int, [C.c_void_p]),
+    "cb_batch_set_phi": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "cb_batch_get_phi": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "cb_batch_scalars": (C.c_int, [C.c_void_p, C.c_int, _P(cb_scalars)]),
+    "cb_batch_run": (C.c_int, [C.c_void_p, C.c_int, _P(cb_run_stats)]),
+    "cb_batch_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(cb_run_stats)]),
+    "cb_serve_trace": (C.c_int, [_P(cb_request), C.c_int, C.c_longlong, C.c_int, C.c_int, _P(cb_result),
+                                 _P(C.c_void_p), _P(cb_serve_stats)]),
     "cb_last_error": (C.c_char_p, []),
     "cb_version": (C.c_char_p, []),
 }
@@ -215,3 +242,78 @@ class Stepper:
         if rc not in (CB_OK, CB_ENONFINITE, CB_EDTUNDERFLOW):
             check(rc)
         return res
+
+
+class Batch:
+    """Many vesicles of uneven grids advanced together (``cb_batch``)."""
+
+    def __init__(self, params_list):
+        arr = (cb_params * len(params_list))(*params_list)
+        h = C.c_void_p()
+        check(lib().cb_batch_create(arr, len(params_list), C.byref(h)))
+        self.h = h
+        self.shapes = [(p.nz, p.nx, p.nx) for p in params_list]
+
+    def close(self):
+        if self.h:
+            lib().cb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.shapes)
+
+    def set_phi(self, i: int, phi: np.ndarray):
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        assert a.shape == self.shapes[i]
+        check(lib().cb_batch_set_phi(self.h, i, _dptr(a), 0))
+
+    def get_phi(self, i: int) -> np.ndarray:
+        out = np.empty(self.shapes[i], np.float64)
+        check(lib().cb_batch_get_phi(self.h, i, _dptr(out), 0))
+        return out
+
+    def scalars(self, i: int) -> dict:
+        s = cb_scalars()
+        check(lib().cb_batch_scalars(self.h, i, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in cb_scalars._fields_}
+
+    def run(self, nsteps: int) -> dict:
+        st = cb_run_stats()
+        check(lib().cb_batch_run(self.h, nsteps, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in cb_run_stats._fields_}
+
+    def run_timed(self, nsteps: int, flush_bytes: int) -> dict:
+        st = cb_run_stats()
+        ms = C.c_double(0)
+        check(lib().cb_batch_run_timed(self.h, nsteps, flush_bytes, C.byref(ms), C.byref(st)))
+        r = {k: getattr(st, k) for k, _ in cb_run_stats._fields_}
+        r["device_ms"] = ms.value
+        return r
+
+
+def serve_trace(requests, hbm_budget_bytes: int, max_slots_per_class: int = 64, quantum: int = 4,
+                phi_out: dict | None = None):
+    """Replay an arrival trace through the continuous-batching server.
+    ``requests``: list of :class:`cb_request`; ``phi_out``: {index: shape} of
+    requests whose final phi to return.  Returns (results, stats, phis)."""
+    n = len(requests)
+    reqs = (cb_request * n)(*requests)
+    res = (cb_result * n)()
+    st = cb_serve_stats()
+    phis = {}
+    ptrs = None
+    if phi_out:
+        ptrs = (C.c_void_p * n)()
+        for i, shape in phi_out.items():
+            phis[i] = np.empty(shape, np.float64)
+            ptrs[i] = phis[i].ctypes.data
+    check(lib().cb_serve_trace(reqs, n, hbm_budget_bytes, max_slots_per_class, quantum, res, ptrs, C.byref(st)))
+    results = [{k: getattr(r, k) for k, _ in cb_result._fields_} for r in res]
+    stats = {k: getattr(st, k) for k, _ in cb_serve_stats._fields_}
+    return results, stats, phis

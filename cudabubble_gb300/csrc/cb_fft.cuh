@@ -13,6 +13,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <type_traits>
 
 namespace cb {
 
@@ -270,29 +271,59 @@ __device__ __forceinline__ void fft_lines_TN(C* buf, int nlines, OFF off, int es
 }
 
 // ------------------------------------------------------------ reductions
+// Sums are carried as FP32 double-float pairs (hi + lo) up to the warp level,
+// so no FP64 instruction runs per thread; only the per-warp partials of a
+// block are added in FP64 (GB300's FP64 rate is a small fraction of FP32).
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float s = a.hi + b.hi;
+    const float bp = s - a.hi;
+    float e = (a.hi - (s - bp)) + (b.hi - bp);  // TwoSum
+    e += a.lo + b.lo;
+    FF r;
+    r.hi = s + e;                                 // FastTwoSum
+    r.lo = e - (r.hi - s);
+    return r;
+}
+__device__ __forceinline__ FF warp_sum(FF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        FF w;
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v = ff_add(v, w);
+    }
+    return v;
+}
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-// Block-wide sum of NV doubles; the result is valid in thread 0.  `red` must
-// hold 32*NV doubles of shared memory.
-template <int NV>
-__device__ __forceinline__ void block_sum(double* v, double* red) {
+// Block-wide sum of NV values (FF pairs or doubles); the FP64 result is valid
+// in thread 0.  `red` must hold 32*NV doubles of shared memory.
+template <int NV, class V>
+__device__ __forceinline__ void block_sum(V* v, double* out, double* red) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
     __syncthreads();
     if (lane == 0) {
 #pragma unroll
-        for (int i = 0; i < NV; ++i) red[i * 32 + w] = v[i];
+        for (int i = 0; i < NV; ++i) {
+            if constexpr (std::is_same<V, FF>::value) red[i * 32 + w] = (double)v[i].hi + (double)v[i].lo;
+            else red[i * 32 + w] = (double)v[i];
+        }
     }
     __syncthreads();
-    if (w == 0) {
+    if (threadIdx.x == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            double s = (lane < nw) ? red[i * 32 + lane] : 0.0;
-            v[i] = warp_sum(s);
+            double s = 0.0;
+            for (int k = 0; k < nw; ++k) s += red[i * 32 + k];
+            out[i] = s;
         }
     }
 }

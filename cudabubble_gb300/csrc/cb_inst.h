@@ -19,6 +19,10 @@ namespace cb {
 
 enum Method { M_EULER = 0, M_ETD2 = 1, M_ETD4 = 2 };
 
+// ETD coefficient tables cached per instance, one per recent dt value
+// (adaptive dt moves among a handful of values: grown, capped, halved)
+constexpr int kNTab = 8;
+
 // which Scal / partial set a kernel works on
 enum Role { R_STATE = 0, R_CAND = 1, R_WORK = 2, R_NROLE = 3 };
 
@@ -35,7 +39,6 @@ struct Scal {
 
 struct Ctrl {
     double dt;        // time step of the next attempt
-    double dt_tab;    // time step the coefficient table was built for (0: none)
     double t;         // accepted time
     double alpha, beta, alpha0, beta0;
     double E_state;   // energy of the accepted state
@@ -52,7 +55,12 @@ struct Ctrl {
     int part_state;   // index (0/1) of the state partial set
     int corr_phase;   // alpha/beta correction sub-step (fixed dt, M != 0)
     int nonfinite;
-    int pad0;
+    int grow_pending;  // apply the dt growth rule at the start of the next attempt
+    int tab_cur;       // coefficient table of the current dt
+    int tab_next;      // round-robin slot for the next new dt
+    int fill_slot;     // table being filled this attempt (-1: none)
+    unsigned fill_cnt; // last-block-done counter of the fill
+    double tab_dt[kNTab];
     unsigned cnt_xy[R_NROLE];  // last-block-done counters per role
     unsigned cnt_z[R_NROLE];
     Scal sc[R_NROLE];
@@ -74,6 +82,25 @@ struct Params {
     double grow_factor, dt_cap, cap_probe, dt_min;
     double tmax;        // Euler loop time limit (belastic.cpp:407)
     double rel_tol;     // > 0: stop once an accepted step changes E by < rel_tol |E|
+    // host-precomputed constants: GB300 runs FP64 at a small fraction of its
+    // FP32 rate, so kernels read these instead of dividing per thread
+    double d_ieps, d_ieps2, d_ieps3, d_bnl;  // 1/eps, 1/eps^2, 1/eps^3, beta * cx
+    float f_eps, f_ieps, f_ieps2, f_ieps3, f_bnl, f_cx, f_invN, f_eta;
+};
+
+// the precomputed constants in the kernel's precision
+template <class T> struct PC;
+template <> struct PC<float> {
+    float eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    __device__ __forceinline__ explicit PC(const Params& p)
+        : eps(p.f_eps), ieps(p.f_ieps), ieps2(p.f_ieps2), ieps3(p.f_ieps3), bnl(p.f_bnl), cx(p.f_cx),
+          invN(p.f_invN), eta(p.f_eta) {}
+};
+template <> struct PC<double> {
+    double eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    __device__ __forceinline__ explicit PC(const Params& p)
+        : eps(p.eps), ieps(p.d_ieps), ieps2(p.d_ieps2), ieps3(p.d_ieps3), bnl(p.d_bnl), cx(p.cx), invN(p.invN),
+          eta(p.eta) {}
 };
 
 // exit reasons kept in Ctrl::status (mirrors the public CB_* codes)
@@ -89,7 +116,7 @@ template <class T> struct InstT {
     void* P[3][2];  // partial sets: [0],[1] state/candidate (swap via ctrl->part_state), [2] work
     void* A;
     void* B;
-    T* coef;
+    T* coef;          // kNTab tables of (kmax + 1) * 8 entries
     Ctrl* ctrl;
     double* part_xy;  // [nz][4] per-plane partial sums
     double* part_z;   // [ntiles][2] per-tile partial sums

@@ -31,11 +31,15 @@ enum ZMode {
 
 enum SpecMul { SM_NONE = 0, SM_LAP = 1, SM_DX = 2, SM_DY = 3, SM_DZ = 4 };
 
+// state_io bits for the plain z modes: the spectrum read (1) or written (2) is
+// a stepped state field (double-float pairs in the FP32 form)
+enum { IO_CIN_STATE = 1, IO_COUT_STATE = 2 };
+
 struct ZArgs {
     int mode;
     int role;      // partial set / Scal record written (stage modes), spectrum read (Z_INV_STATE)
     int mul;       // SpecMul for Z_INV_PLAIN
-    int pad;
+    int state_io;  // IO_* bits (Z_FWD_PLAIN / Z_INV_PLAIN)
     const void* cin;
     void* cout;
 };

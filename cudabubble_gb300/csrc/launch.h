@@ -15,8 +15,9 @@ template <class T> struct Launch {
     static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s);
     static cudaError_t z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s);
     static cudaError_t decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s);
-    static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s);
+    static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw = 1);
     static cudaError_t to_double(const void* in, double* out, size_t n, cudaStream_t s);
+    static cudaError_t state_to_double(const void* in, double* out, size_t n, cudaStream_t s);
 };
 
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,

@@ -94,13 +94,22 @@ template <class T> cudaError_t Launch<T>::decide(const InstT<T>* d, int ninst, i
     decide_kernel<T><<<(ninst + 127) / 128, 128, 0, s>>>(d, ninst, raw);
     return cudaGetLastError();
 }
-template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s) {
-    coef_kernel<T><<<ninst, 512, 0, s>>>(d, accurate);
+template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw) {
+    prologue_kernel<T><<<(ninst + 127) / 128, 128, 0, s>>>(d, ninst, raw);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    coef_fill_kernel<T><<<dim3(64, ninst), 256, 0, s>>>(d, accurate);
     return cudaGetLastError();
 }
 template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out, size_t n, cudaStream_t s) {
     const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     cplx_to_double_kernel<T><<<blocks, 256, 0, s>>>(reinterpret_cast<const cplx<T>*>(in), reinterpret_cast<double2*>(out), n);
+    return cudaGetLastError();
+}
+
+template <class T> cudaError_t Launch<T>::state_to_double(const void* in, double* out, size_t n, cudaStream_t s) {
+    const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    state_to_double_kernel<T><<<blocks, 256, 0, s>>>(in, reinterpret_cast<double2*>(out), n);
     return cudaGetLastError();
 }
 

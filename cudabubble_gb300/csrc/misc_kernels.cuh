@@ -8,81 +8,130 @@
 
 namespace cb {
 
-// phi_1..3(z) = sum_j z^j / (j+k)!  (Taylor for |z| < 1, closed forms otherwise)
+// 1 / m! as compile-time constants (m <= 27)
+__host__ __device__ constexpr double rfact(int m) { return m <= 1 ? 1.0 : rfact(m - 1) / (double)m; }
+
+// phi_k(z) = sum_j z^j / (j+k)!, k = 1, 2, 3: Horner series for |z| < 1
+// (24 terms, no divisions), closed forms otherwise
 __device__ inline void phi123(double z, double& p1, double& p2, double& p3) {
     if (fabs(z) < 1.0) {
-        double t1 = 0.0, t2 = 0.0, t3 = 0.0, zp = 1.0, f1 = 1.0, f2 = 2.0, f3 = 6.0;
-        for (int j = 0; j < 24; ++j) {
-            t1 += zp / f1;
-            t2 += zp / f2;
-            t3 += zp / f3;
-            zp *= z;
-            f1 *= (double)(j + 2);
-            f2 *= (double)(j + 3);
-            f3 *= (double)(j + 4);
+        double t1 = rfact(24), t2 = rfact(25), t3 = rfact(26);
+#pragma unroll
+        for (int j = 23; j >= 0; --j) {
+            t1 = fma(t1, z, rfact(j + 1));
+            t2 = fma(t2, z, rfact(j + 2));
+            t3 = fma(t3, z, rfact(j + 3));
         }
         p1 = t1; p2 = t2; p3 = t3;
     } else {
-        const double ez = exp(z);
-        p1 = (ez - 1.0) / z;
-        p2 = (ez - 1.0 - z) / (z * z);
-        p3 = (ez - 1.0 - z - 0.5 * z * z) / (z * z * z);
+        const double ez = exp(z), iz = 1.0 / z;
+        p1 = (ez - 1.0) * iz;
+        p2 = (p1 - 1.0) * iz;
+        p3 = (p2 - 0.5) * iz;
     }
 }
 
-// Builds the per-|k|^2 coefficient table for the current dt, once per dt.
+// Prologue of every attempt (one thread per instance).  It applies a pending
+// growth of dt (set when the accepted step count reached a multiple of
+// grow_every: belastic.cpp:644-651, :376-378), so the step runs with the grown
+// dt exactly as the reference's loop head grows it, then selects the
+// coefficient table of the attempt's dt from the per-instance cache, marking
+// a slot for filling on a miss.
+template <class T>
+__global__ void prologue_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const InstT<T>& I = insts[i];
+    Ctrl* c = I.ctrl;
+    const Params& p = I.p;
+    if (c->done) return;
+    if (!raw && c->grow_pending) {
+        const double d0 = c->dt;
+        c->dt = (d0 * p.cap_probe < p.dt_cap) ? d0 * p.grow_factor : p.dt_cap;
+        c->grow_pending = 0;
+    }
+    c->fill_slot = -1;
+    if (p.method == M_EULER) return;
+    for (int j = 0; j < kNTab; ++j)
+        if (c->tab_dt[j] == c->dt) { c->tab_cur = j; return; }
+    const int j = c->tab_next;
+    c->tab_next = (j + 1) % kNTab;
+    c->tab_dt[j] = c->dt;
+    c->tab_cur = j;
+    c->fill_slot = j;
+}
+
+// Fills the table slot the prologue selected (grid: blocks x instances).
 // L(k) follows Calc.cu:579-606 with c = -cx |k|^2 (kappa = 2, D = 1.5).
 // accurate == 0 evaluates the reference's own closed forms (Calc.cu:446-569);
 // accurate == 1 uses phi-functions, free of the small-|hL| cancellation.
+// The FP32 form stores em = exp(hL) - 1 in place of the exponential factors
+// (slots 0 and 2): its state update is base + (em base + increment) in
+// double-float arithmetic (z_kernel.cuh, State<float>).
 template <class T>
-__global__ void coef_kernel(const InstT<T>* __restrict__ insts, int accurate) {
-    const InstT<T>& I = insts[blockIdx.x];
+__global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurate) {
+    const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
-    if (p.method == M_EULER) return;
-    const double dt = ctrl->dt;
-    if (ctrl->dt_tab == dt) return;
-    const double kappa = 2.0, D = 1.5, eps = p.eps;
-    for (int idx = threadIdx.x; idx <= p.kmax; idx += blockDim.x) {
+    if (p.method == M_EULER || ctrl->done) return;
+    const int slot = ctrl->fill_slot;
+    if (slot < 0) return;
+    const double dt = ctrl->tab_dt[slot];
+    const double kappa = 2.0, D = 1.5, eps = p.eps, ie = p.d_ieps, ie2 = p.d_ieps2;
+    T* tab = I.coef + (size_t)slot * (size_t)(p.kmax + 1) * 8;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx <= p.kmax; idx += gridDim.x * blockDim.x) {
         const double c = -(double)idx * p.cx;
-        const double L = -eps * c * c + kappa * c / eps + D * (c - kappa / (eps * eps)) / eps;
-        T* out = I.coef + 8 * (size_t)idx;
+        const double L = -eps * c * c + kappa * c * ie + D * (c - kappa * ie2) * ie;
+        T* out = tab + 8 * (size_t)idx;
         if (p.method == M_ETD2) {
-            double e1 = exp(L * dt), c1, c2;
+            double x0, c1, c2;
             if (accurate) {
                 double p1, p2, p3;
                 phi123(dt * L, p1, p2, p3);
                 c1 = dt * p1;
                 c2 = dt * p2;
+                x0 = (sizeof(T) == 4) ? dt * L * p1 : exp(L * dt);
             } else {
+                const double e1 = exp(L * dt);
                 c1 = (e1 - 1.0) / L;
                 c2 = (dt * L == 0.0) ? dt / 2 : (e1 - 1.0 - dt * L) / (dt * L * L);
+                x0 = (sizeof(T) == 4) ? e1 - 1.0 : e1;
             }
-            out[0] = (T)e1; out[1] = (T)c1; out[2] = (T)c2;
+            out[0] = (T)x0; out[1] = (T)c1; out[2] = (T)c2;
         } else {
-            const double eh = exp(L * dt / 2), e2 = eh * eh;
-            double ch, f1, f2, f3;
+            double x0, x2, ch, f1, f2, f3;
             if (accurate) {
-                double p1, p2, p3;
-                phi123(dt * L / 2, p1, p2, p3);
-                ch = dt / 2 * p1;
+                double q1, q2, q3, p1, p2, p3;
+                phi123(dt * L / 2, q1, q2, q3);
                 phi123(dt * L, p1, p2, p3);
+                ch = dt / 2 * q1;
                 f1 = dt * (p1 - 3.0 * p2 + 4.0 * p3);
                 f2 = 2.0 * dt * (p2 - 2.0 * p3);
                 f3 = dt * (4.0 * p3 - p2);
+                x0 = (sizeof(T) == 4) ? dt * L / 2 * q1 : exp(L * dt / 2);
+                x2 = (sizeof(T) == 4) ? dt * L * p1 : exp(L * dt);
             } else {
-                const double h = dt;
+                const double eh = exp(L * dt / 2), e2 = eh * eh, h = dt;
                 const double q = 1.0 / (h * h * L * L * L);
                 ch = (eh - 1.0) / L;
                 f1 = q * (-4.0 - h * L + e2 * (4.0 - 3.0 * h * L + h * h * L * L));
                 f2 = q * 2.0 * (2.0 + h * L + e2 * (-2.0 + h * L));
                 f3 = q * (-4.0 - 3.0 * h * L - h * h * L * L + e2 * (4.0 - h * L));
+                x0 = (sizeof(T) == 4) ? eh - 1.0 : eh;
+                x2 = (sizeof(T) == 4) ? e2 - 1.0 : e2;
             }
-            out[0] = (T)eh; out[1] = (T)ch; out[2] = (T)e2; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
+            out[0] = (T)x0; out[1] = (T)ch; out[2] = (T)x2; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) ctrl->dt_tab = dt;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&ctrl->fill_cnt, 1u);
+        if (prev == gridDim.x - 1) {
+            ctrl->fill_cnt = 0u;
+            ctrl->fill_slot = -1;
+        }
+    }
 }
 
 // Accept / reject after one attempt (one thread per instance).
@@ -129,7 +178,11 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     c->spec_state ^= 1;
     c->part_state ^= 1;
     c->sc[R_STATE] = cs;
-    c->E_state = E1;
+    if (!raw && p.corr) {  // the energy against the corrected targets (belastic.cpp:68-86)
+        const double ve = cs.V - c->alpha, se = cs.S - c->beta;
+        c->sc[R_STATE].E = p.eta * cs.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
+    }
+    c->E_state = c->sc[R_STATE].E;
     c->fresh = 1;
     const bool nonfinite = !isfinite(E1) || !isfinite(cs.V) || !isfinite(cs.S);
     if (nonfinite) { c->done = 1; c->status = ST_NONFINITE; c->nonfinite = 1; return; }
@@ -147,8 +200,7 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     if (c->steps >= c->target) { c->done = 1; c->status = ST_TARGET; }
     // relaxation criterion |dE / E| < rel_tol (no counterpart in the reference loops)
     if (!raw && p.rel_tol > 0.0 && fabs(E1 - E0) < p.rel_tol * fabs(E1)) { c->done = 1; c->status = ST_CONVERGED; }
-    if (!raw && p.adaptive && c->steps % p.grow_every == 0)
-        c->dt = (c->dt * p.cap_probe < p.dt_cap) ? c->dt * p.grow_factor : p.dt_cap;
+    if (!raw && p.adaptive && c->steps % p.grow_every == 0) c->grow_pending = 1;
 }
 
 // ---------------------------------------------------------- slow path
@@ -174,6 +226,19 @@ static __global__ void pointwise_kernel(int kind, size_t n, double* out, const d
                 break;
             }
             case PW_RHS: out[i] = x0 * 0.5 + x1 * b[i] + c[i] * x2; break;                    // a unused, b = f, c = g0
+        }
+    }
+}
+
+// stepped-state spectrum (FP64, or double-float pairs in the FP32 form) -> complex double
+template <class T>
+__global__ void state_to_double_kernel(const void* __restrict__ in, double2* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (sizeof(T) == 4) {
+            const float4 q = reinterpret_cast<const float4*>(in)[i];
+            out[i] = make_double2((double)q.x + (double)q.z, (double)q.y + (double)q.w);
+        } else {
+            out[i] = reinterpret_cast<const double2*>(in)[i];
         }
     }
 }

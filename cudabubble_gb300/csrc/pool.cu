@@ -1,0 +1,574 @@
+// Batched and served pools of stepper instances.
+//
+// Instances that share (grid, method, coefficient mode) form a size class.
+// A class owns a fixed-capacity device table of instance descriptors; one
+// launch per pass covers every slot of the class (blockIdx.y = slot), and one
+// captured CUDA graph runs one attempt of every class, each class on its own
+// forked stream.  An empty slot points at a control block that is always
+// done, so its CTAs return at once; admitting or retiring an instance only
+// rewrites one table entry and the graph is never re-captured.  Every slot
+// keeps its own dt, accept/reject state and FP64 scalars, so an instance's
+// result is the same alone and in any mix.
+//
+// The reference runs one grid per process (main.cpp:17-18) and has no batched
+// or served mode; these are additions of this implementation.
+#include <chrono>
+#include <deque>
+#include <thread>
+
+#include "stepper.cuh"
+
+namespace cb {
+
+struct SlotSummary {
+    int done, status, steps, attempts, rejects, pad;
+    double E, dt;
+};
+
+template <class T>
+__global__ void gather_kernel(const InstT<T>* __restrict__ table, int cap, SlotSummary* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    const Ctrl* c = table[i].ctrl;
+    SlotSummary s;
+    s.done = c->done;
+    s.status = c->status;
+    s.steps = c->steps;
+    s.attempts = c->attempts;
+    s.rejects = c->rejects;
+    s.pad = 0;
+    s.E = c->E_state;
+    s.dt = c->dt;
+    out[i] = s;
+}
+
+// phi0 = tanh(d / (sqrt(2) eps)) of one ellipsoid or the union of two
+// (d = max(d1, d2)), on the grid x_i = i L / n - L / 2 (fluidbase.cpp:156-161).
+__global__ void ellipsoid_kernel(double* __restrict__ out, int nx, int nz, double L, double eps, double a0,
+                                 double a1, double a2, double c0, double c1, double c2, double b0, double b1,
+                                 double b2, double e0, double e1, double e2) {
+    const size_t n = (size_t)nx * nx * nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx), y = (int)((i / nx) % nx), z = (int)(i / ((size_t)nx * nx));
+        const double X = x * L / nx - L / 2.0, Y = y * L / nx - L / 2.0, Z = z * L / nz - L / 2.0;
+        const double u = (X - c0) / a0, v = (Y - c1) / a1, w = (Z - c2) / a2;
+        double d = (1.0 - sqrt(u * u + v * v + w * w)) * fmin(a0, fmin(a1, a2));
+        if (b0 > 0) {
+            const double u2 = (X - e0) / b0, v2 = (Y - e1) / b1, w2 = (Z - e2) / b2;
+            d = fmax(d, (1.0 - sqrt(u2 * u2 + v2 * v2 + w2 * w2)) * fmin(b0, fmin(b1, b2)));
+        }
+        out[i] = tanh(d / (sqrt(2.0) * eps));
+    }
+}
+
+template <class T> struct PoolClass {
+    int nx = 0, nz = 0, method = 0, accurate = 0, cap = 0, ntiles = 0;
+    InstT<T>* table = nullptr;
+    SlotSummary* sum = nullptr;
+    std::vector<Stepper<T>*> occ;
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+template <class T> class Pool {
+   public:
+    ~Pool() {
+        if (st) cudaStreamSynchronize(st);
+        if (g) cudaGraphExecDestroy(g);
+        for (auto& c : cls) {
+            cudaFree(c.table);
+            cudaFree(c.sum);
+            if (c.s) cudaStreamDestroy(c.s);
+            if (c.fork) cudaEventDestroy(c.fork);
+            if (c.join) cudaEventDestroy(c.join);
+        }
+        cudaFree(dummy_ctrl);
+        cudaFreeHost(h_sum);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int init() {
+        CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        CB_CK(cudaMalloc(&dummy_ctrl, sizeof(Ctrl)));
+        Ctrl c;
+        memset(&c, 0, sizeof c);
+        c.done = 1;
+        CB_CK(cudaMemcpy(dummy_ctrl, &c, sizeof c, cudaMemcpyHostToDevice));
+        memset(&dummy, 0, sizeof dummy);
+        dummy.ctrl = dummy_ctrl;
+        return CB_OK;
+    }
+
+    int find(int nx, int nz, int method, int accurate) const {
+        for (size_t i = 0; i < cls.size(); ++i)
+            if (cls[i].nx == nx && cls[i].nz == nz && cls[i].method == method && cls[i].accurate == accurate)
+                return (int)i;
+        return -1;
+    }
+
+    int add_class(int nx, int nz, int method, int accurate, int ntiles, int cap) {
+        if (g) return fail(CB_EINVAL, "pool graph already built");
+        PoolClass<T> c;
+        c.nx = nx; c.nz = nz; c.method = method; c.accurate = accurate; c.cap = cap; c.ntiles = ntiles;
+        c.occ.assign(cap, nullptr);
+        CB_CK(cudaMalloc(&c.table, sizeof(InstT<T>) * cap));
+        CB_CK(cudaMalloc(&c.sum, sizeof(SlotSummary) * cap));
+        std::vector<InstT<T>> init(cap, dummy);
+        CB_CK(cudaMemcpy(c.table, init.data(), sizeof(InstT<T>) * cap, cudaMemcpyHostToDevice));
+        CB_CK(cudaStreamCreateWithFlags(&c.s, cudaStreamNonBlocking));
+        CB_CK(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+        CB_CK(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
+        cls.push_back(c);
+        return CB_OK;
+    }
+
+    // put an instance into a free slot of its class
+    int place(Stepper<T>* sp, int* ci, int* si) {
+        const Params& p = sp->params();
+        const int c = find(p.nx, p.nz, p.method, sp->accurate());
+        if (c < 0) return fail(CB_EINVAL, "no size class for %dx%dx%d", p.nx, p.ny, p.nz);
+        for (int k = 0; k < cls[c].cap; ++k) {
+            if (!cls[c].occ[k]) {
+                cls[c].occ[k] = sp;
+                CB_CK(cudaMemcpyAsync(cls[c].table + k, &sp->inst(), sizeof(InstT<T>), cudaMemcpyHostToDevice, st));
+                CB_CK(cudaStreamSynchronize(st));
+                *ci = c;
+                *si = k;
+                return CB_OK;
+            }
+        }
+        return fail(CB_ENOMEM, "size class full");
+    }
+
+    bool has_free(int c) const {
+        for (auto* o : cls[c].occ)
+            if (!o) return true;
+        return false;
+    }
+
+    int release(int c, int k) {
+        cls[c].occ[k] = nullptr;
+        CB_CK(cudaMemcpyAsync(cls[c].table + k, &dummy, sizeof(InstT<T>), cudaMemcpyHostToDevice, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    int build_graph() {
+        int total = 0;
+        for (auto& c : cls) total += c.cap;
+        CB_CK(cudaMallocHost(&h_sum, sizeof(SlotSummary) * (total > 0 ? total : 1)));
+        cudaGraph_t gr = nullptr;
+        CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t r = cudaSuccess;
+        for (auto& c : cls) {
+            if (r == cudaSuccess) r = cudaEventRecord(c.fork, st);
+            if (r == cudaSuccess) r = cudaStreamWaitEvent(c.s, c.fork, 0);
+            if (r == cudaSuccess)
+                r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false, c.s);
+            if (r == cudaSuccess) r = cudaEventRecord(c.join, c.s);
+            if (r == cudaSuccess) r = cudaStreamWaitEvent(st, c.join, 0);
+        }
+        cudaError_t e = cudaStreamEndCapture(st, &gr);
+        if (r != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return fail(CB_ECUDA, "pool capture: %s", cudaGetErrorString(r));
+        }
+        CB_CK(e);
+        cudaError_t ie = cudaGraphInstantiate(&g, gr, 0);
+        cudaGraphDestroy(gr);
+        CB_CK(ie);
+        return CB_OK;
+    }
+
+    cudaError_t launch(int attempts) {
+        for (int i = 0; i < attempts; ++i) {
+            cudaError_t r = cudaGraphLaunch(g, st);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    }
+
+    // per-slot summaries of every class (class-major), synchronises the pool stream
+    int poll(std::vector<SlotSummary>& out) {
+        int off = 0;
+        for (auto& c : cls) {
+            gather_kernel<T><<<(c.cap + 127) / 128, 128, 0, st>>>(c.table, c.cap, c.sum);
+            CB_CK(cudaGetLastError());
+            CB_CK(cudaMemcpyAsync(h_sum + off, c.sum, sizeof(SlotSummary) * c.cap, cudaMemcpyDeviceToHost, st));
+            off += c.cap;
+        }
+        CB_CK(cudaStreamSynchronize(st));
+        out.assign(h_sum, h_sum + off);
+        return CB_OK;
+    }
+
+    int slot_index(int c, int k) const {
+        int off = 0;
+        for (int i = 0; i < c; ++i) off += cls[i].cap;
+        return off + k;
+    }
+    cudaStream_t stream() const { return st; }
+    std::vector<PoolClass<T>> cls;
+
+   private:
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t g = nullptr;
+    Ctrl* dummy_ctrl = nullptr;
+    InstT<T> dummy{};
+    SlotSummary* h_sum = nullptr;
+};
+
+// ---------------------------------------------------------------- batch
+struct BatchBase {
+    virtual ~BatchBase() {}
+    virtual int set_phi(int i, const double* phi, bool dev) = 0;
+    virtual int get_phi(int i, double* phi, bool dev) = 0;
+    virtual int scalars(int i, cb_scalars* s) = 0;
+    virtual int run(int nsteps, cb_run_stats* st, long long flush_bytes, double* ms) = 0;
+    virtual int size() const = 0;
+};
+
+template <class T> class Batch final : public BatchBase {
+   public:
+    ~Batch() override {
+        pool.reset();
+        items.clear();
+        cudaFree(flush_buf);
+    }
+    int init(const cb_params* ps, int n) {
+        pool.reset(new Pool<T>());
+        int rc = pool->init();
+        if (rc) return rc;
+        for (int i = 0; i < n; ++i) {
+            std::unique_ptr<Stepper<T>> s(new Stepper<T>());
+            rc = s->init(ps[i]);
+            if (rc) return rc;
+            items.push_back(std::move(s));
+        }
+        for (auto& it : items) {
+            const Params& p = it->params();
+            if (pool->find(p.nx, p.nz, p.method, it->accurate()) >= 0) continue;
+            int cap = 0;
+            for (auto& jt : items) {
+                const Params& q = jt->params();
+                if (q.nx == p.nx && q.nz == p.nz && q.method == p.method && jt->accurate() == it->accurate()) ++cap;
+            }
+            rc = pool->add_class(p.nx, p.nz, p.method, it->accurate(), it->tiles(), cap);
+            if (rc) return rc;
+        }
+        where.resize(n);
+        for (int i = 0; i < n; ++i) {
+            rc = pool->place(items[i].get(), &where[i].first, &where[i].second);
+            if (rc) return rc;
+        }
+        return pool->build_graph();
+    }
+    int size() const override { return (int)items.size(); }
+    int set_phi(int i, const double* phi, bool dev) override { return items[i]->set_phi(phi, dev); }
+    int get_phi(int i, double* phi, bool dev) override { return items[i]->get_phi(phi, dev); }
+    int scalars(int i, cb_scalars* s) override { return items[i]->scalars(s); }
+
+    // every instance advances nsteps accepted steps (or stops on its own exit
+    // test); flush_bytes > 0 times attempt by attempt with an L2 flush between
+    int run(int nsteps, cb_run_stats* stt, long long flush_bytes, double* ms_out) override {
+        int steps0 = 0, att0 = 0;
+        for (auto& it : items) {
+            cb_scalars s;
+            int rc = it->scalars(&s);
+            if (rc) return rc;
+            steps0 += s.steps;
+            att0 += s.attempts;
+            rc = it->prepare_run(nsteps);
+            if (rc) return rc;
+        }
+        if (flush_bytes > 0 && flush_bytes != flush_size) {
+            cudaFree(flush_buf);
+            flush_buf = nullptr;
+            CB_CK(cudaMalloc(&flush_buf, (size_t)flush_bytes));
+            flush_size = flush_bytes;
+        }
+        cudaStream_t s = pool->stream();
+        cudaEvent_t e0, e1;
+        CB_CK(cudaEventCreate(&e0));
+        CB_CK(cudaEventCreate(&e1));
+        double total = 0.0;
+        int launches = 0;
+        const long long limit = 70LL * (nsteps + 1) * 2 + 1000;
+        std::vector<SlotSummary> sum;
+        bool all = false;
+        CB_CK(cudaEventRecord(e0, s));
+        while (!all && launches < limit) {
+            const int chunk = flush_bytes > 0 ? 1 : 8;
+            if (flush_bytes > 0) {
+                CB_CK(cudaMemsetAsync(flush_buf, launches & 0xff, (size_t)flush_bytes, s));
+                CB_CK(cudaEventRecord(e0, s));
+            }
+            CB_CK(pool->launch(chunk));
+            launches += chunk;
+            if (flush_bytes > 0) {
+                CB_CK(cudaEventRecord(e1, s));
+                CB_CK(cudaEventSynchronize(e1));
+                float m = 0.f;
+                cudaEventElapsedTime(&m, e0, e1);
+                total += m;
+            }
+            int rc = pool->poll(sum);
+            if (rc) return rc;
+            all = true;
+            for (auto& w : where)
+                if (!sum[pool->slot_index(w.first, w.second)].done) { all = false; break; }
+        }
+        if (flush_bytes <= 0) {
+            CB_CK(cudaEventRecord(e1, s));
+            CB_CK(cudaEventSynchronize(e1));
+            float m = 0.f;
+            cudaEventElapsedTime(&m, e0, e1);
+            total = m;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int steps1 = 0, att1 = 0, worst = ST_TARGET;
+        for (auto& it : items) {
+            int status = 0;
+            int rc = it->finish_run(&status);
+            if (rc) return rc;
+            cb_scalars sc;
+            it->scalars(&sc);
+            steps1 += sc.steps;
+            att1 += sc.attempts;
+            if (status != ST_TARGET) worst = status;
+        }
+        if (stt) {
+            stt->steps = steps1 - steps0;
+            stt->attempts = att1 - att0;
+            stt->status = worst;
+            stt->graph_launches = launches;
+            stt->device_ms = total;
+        }
+        if (ms_out) *ms_out = total;
+        if (launches >= limit) return fail(CB_ENOTCONVERGED, "batch made no progress");
+        return CB_OK;
+    }
+
+   private:
+    std::unique_ptr<Pool<T>> pool;
+    std::vector<std::unique_ptr<Stepper<T>>> items;
+    std::vector<std::pair<int, int>> where;
+    void* flush_buf = nullptr;
+    long long flush_size = 0;
+};
+
+// ---------------------------------------------------------------- server
+template <class T>
+static int make_phi0(Stepper<T>& s, const cb_request& r, double* stage) {
+    const Params& p = s.params();
+    const double L = (r.params.lenx > 0 ? r.params.lenx : 1.0) * kTwoPi;
+    ellipsoid_kernel<<<1024, 256>>>(stage, p.nx, p.nz, L, p.eps, r.axes[0], r.axes[1], r.axes[2], r.centre[0],
+                                    r.centre[1], r.centre[2], r.axes2[0], r.axes2[1], r.axes2[2], r.centre2[0],
+                                    r.centre2[1], r.centre2[2]);
+    CB_CK(cudaGetLastError());
+    CB_CK(cudaDeviceSynchronize());
+    return s.set_phi(stage, true);
+}
+
+template <class T> struct Active {
+    std::unique_ptr<Stepper<T>> st;
+    int req, cls, slot;
+    long long bytes;
+};
+
+// Continuous batching over an arrival trace, in real time: arrivals join a
+// FIFO queue; the head is admitted while its class has a free slot and the
+// HBM budget holds its instance; every loop iteration runs `quantum`
+// attempts of all admitted instances; finished ones are retired at once.
+template <class T>
+static int serve_impl(const cb_request* reqs, int n, long long budget, int max_slots, int quantum, cb_result* res,
+                      double** phi_out, cb_serve_stats* stats) {
+    Pool<T> pool;
+    int rc = pool.init();
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) {  // size classes of the trace
+        Eff e;
+        rc = make_params(reqs[i].params, e);
+        if (rc) return rc;
+        if (!Launch<T>::xy_supported(e.p.nx) || !Launch<T>::z_supported(e.p.nz))
+            return fail(CB_EUNSUPPORTED, "request %d: grid %d^2x%d not built", i, e.p.nx, e.p.nz);
+        if (pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate) >= 0) continue;
+        const long long bytes = (long long)instance_arena_bytes<T>(e.p);
+        int cap = (int)std::min<long long>(max_slots, budget / std::max<long long>(bytes, 1));
+        cap = std::max(cap, 1);
+        const int tx = Launch<T>::z_tile();
+        rc = pool.add_class(e.p.nx, e.p.nz, e.p.method, e.accurate, (e.p.ny * e.p.nc + tx - 1) / tx, cap);
+        if (rc) return rc;
+    }
+    rc = pool.build_graph();
+    if (rc) return rc;
+    double* stage = nullptr;
+    long long maxN = 0;
+    for (int i = 0; i < n; ++i)
+        maxN = std::max<long long>(maxN, (long long)reqs[i].params.nx * reqs[i].params.nx * reqs[i].params.nz);
+    CB_CK(cudaMalloc(&stage, (size_t)maxN * sizeof(double)));
+
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto now = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reqs[a].arrival_s < reqs[b].arrival_s; });
+    size_t next = 0;
+    std::deque<int> queue;
+    std::vector<Active<T>> act;
+    long long used = 0, peak = 0;
+    int done = 0, launches = 0;
+    double point_steps = 0.0;
+    std::vector<SlotSummary> sum;
+    while (done < n) {
+        const double tnow = now();
+        while (next < order.size() && reqs[order[next]].arrival_s <= tnow) queue.push_back(order[next++]);
+        // admission (FIFO, head of line)
+        while (!queue.empty()) {
+            const int i = queue.front();
+            Eff e;
+            make_params(reqs[i].params, e);
+            const long long bytes = (long long)instance_arena_bytes<T>(e.p);
+            const int c = pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate);
+            if (used + bytes > budget || !pool.has_free(c)) break;
+            Active<T> a;
+            a.st.reset(new Stepper<T>());
+            rc = a.st->init(reqs[i].params);
+            if (rc == CB_OK) rc = make_phi0(*a.st, reqs[i], stage);
+            if (rc == CB_OK) rc = a.st->prepare_run(reqs[i].max_steps > 0 ? reqs[i].max_steps : INT_MAX / 2);
+            if (rc == CB_OK) rc = pool.place(a.st.get(), &a.cls, &a.slot);
+            if (rc) { cudaFree(stage); return rc; }
+            a.req = i;
+            a.bytes = bytes;
+            used += bytes;
+            peak = std::max(peak, used);
+            res[i].arrival_s = reqs[i].arrival_s;
+            res[i].admitted_s = now();
+            res[i].bytes = bytes;
+            queue.pop_front();
+            act.push_back(std::move(a));
+        }
+        if (act.empty()) {
+            if (next < order.size()) {
+                const double wait = reqs[order[next]].arrival_s - now();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            }
+            continue;
+        }
+        cudaError_t le = pool.launch(quantum);
+        if (le != cudaSuccess) { cudaFree(stage); return fail(CB_ECUDA, "pool launch: %s", cudaGetErrorString(le)); }
+        launches += quantum;
+        rc = pool.poll(sum);
+        if (rc) { cudaFree(stage); return rc; }
+        for (size_t j = 0; j < act.size();) {
+            const SlotSummary& s = sum[pool.slot_index(act[j].cls, act[j].slot)];
+            if (!s.done) { ++j; continue; }
+            Active<T>& a = act[j];
+            const int i = a.req;
+            int status = 0;
+            a.st->finish_run(&status);
+            cb_scalars sc;
+            a.st->scalars(&sc);
+            res[i].finished_s = now();
+            res[i].latency_s = res[i].finished_s - res[i].arrival_s;
+            res[i].E = sc.E;
+            res[i].V = sc.V;
+            res[i].S = sc.S;
+            res[i].steps = sc.steps;
+            res[i].attempts = sc.attempts;
+            res[i].status = status;
+            point_steps += (double)a.st->params().N * sc.steps;
+            if (phi_out && phi_out[i]) a.st->get_phi(phi_out[i], false);
+            pool.release(a.cls, a.slot);
+            used -= a.bytes;
+            act.erase(act.begin() + j);
+            ++done;
+        }
+    }
+    cudaFree(stage);
+    if (stats) {
+        stats->wall_s = now();
+        stats->completed = done;
+        stats->point_steps = point_steps;
+        stats->graph_launches = launches;
+        stats->peak_bytes = peak;
+    }
+    return CB_OK;
+}
+
+}  // namespace cb
+
+// ====================================================================== C ABI
+struct cb_batch {
+    std::unique_ptr<cb::BatchBase> impl;
+};
+
+extern "C" {
+
+int cb_batch_create(const cb_params* ps, int n, cb_batch** out) {
+    if (!ps || n <= 0 || !out) return cb::fail(CB_EINVAL, "bad batch arguments");
+    *out = nullptr;
+    for (int i = 1; i < n; ++i)
+        if (ps[i].precision != ps[0].precision) return cb::fail(CB_EINVAL, "a batch holds one precision");
+    std::unique_ptr<cb_batch> b(new cb_batch);
+    int rc;
+    if (ps[0].precision == CB_FP32) {
+        auto* p = new cb::Batch<float>();
+        b->impl.reset(p);
+        rc = p->init(ps, n);
+    } else {
+        auto* p = new cb::Batch<double>();
+        b->impl.reset(p);
+        rc = p->init(ps, n);
+    }
+    if (rc) return rc;
+    *out = b.release();
+    return CB_OK;
+}
+
+int cb_batch_destroy(cb_batch* b) {
+    delete b;
+    return CB_OK;
+}
+
+#define CB_B(b, i) \
+    if (!(b) || !(b)->impl || (i) < 0 || (i) >= (b)->impl->size()) return cb::fail(CB_EINVAL, "bad batch index")
+
+int cb_batch_set_phi(cb_batch* b, int i, const double* phi, int on_device) {
+    CB_B(b, i);
+    return b->impl->set_phi(i, phi, on_device != 0);
+}
+int cb_batch_get_phi(cb_batch* b, int i, double* phi, int on_device) {
+    CB_B(b, i);
+    return b->impl->get_phi(i, phi, on_device != 0);
+}
+int cb_batch_scalars(cb_batch* b, int i, cb_scalars* s) {
+    CB_B(b, i);
+    return b->impl->scalars(i, s);
+}
+int cb_batch_run(cb_batch* b, int nsteps, cb_run_stats* st) {
+    CB_B(b, 0);
+    return b->impl->run(nsteps, st, 0, nullptr);
+}
+int cb_batch_run_timed(cb_batch* b, int nsteps, long long flush_bytes, double* device_ms, cb_run_stats* st) {
+    CB_B(b, 0);
+    return b->impl->run(nsteps, st, flush_bytes, device_ms);
+}
+
+int cb_serve_trace(const cb_request* reqs, int n, long long hbm_budget_bytes, int max_slots_per_class, int quantum,
+                   cb_result* results, double** phi_out, cb_serve_stats* stats) {
+    if (!reqs || n <= 0 || !results || hbm_budget_bytes <= 0) return cb::fail(CB_EINVAL, "bad serve arguments");
+    memset(results, 0, sizeof(cb_result) * (size_t)n);
+    for (int i = 1; i < n; ++i)
+        if (reqs[i].params.precision != reqs[0].params.precision)
+            return cb::fail(CB_EINVAL, "a trace holds one precision");
+    const int q = quantum > 0 ? quantum : 4;
+    const int ms = max_slots_per_class > 0 ? max_slots_per_class : 64;
+    if (reqs[0].params.precision == CB_FP32)
+        return cb::serve_impl<float>(reqs, n, hbm_budget_bytes, ms, q, results, phi_out, stats);
+    return cb::serve_impl<double>(reqs, n, hbm_budget_bytes, ms, q, results, phi_out, stats);
+}
+
+}  // extern "C"

@@ -146,6 +146,21 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.dt_min = 1e-23;
     p.tmax = u.tmax >= 0 ? u.tmax : 4.0;
     p.rel_tol = u.rel_tol > 0 ? u.rel_tol : 0.0;
+    // nonlinear term N-hat = A-hat + beta cx |k|^2 B-hat: beta = eta (Euler, -lap f in g0)
+    // or -eta/eps (ETD, +lap t / eps in -eta NL)
+    const double beta = euler ? p.eta : -p.eta / p.eps;
+    p.d_ieps = 1.0 / p.eps;
+    p.d_ieps2 = 1.0 / (p.eps * p.eps);
+    p.d_ieps3 = 1.0 / (p.eps * p.eps * p.eps);
+    p.d_bnl = beta * p.cx;
+    p.f_eps = (float)p.eps;
+    p.f_ieps = (float)p.d_ieps;
+    p.f_ieps2 = (float)p.d_ieps2;
+    p.f_ieps3 = (float)p.d_ieps3;
+    p.f_bnl = (float)p.d_bnl;
+    p.f_cx = (float)p.cx;
+    p.f_invN = (float)p.invN;
+    p.f_eta = (float)p.eta;
     const double ts = u.time_step > 0 ? u.time_step : 1e-6;  // fluidbase.cpp:112
     e.dt0 = p.adaptive ? ts : std::min(u.fixed_time_step, ts);  // belastic.cpp:599-602
     e.precision = u.precision;
@@ -212,6 +227,8 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             return Launch<T>::z(nz, d, ninst, ntiles, a, s);
         });
     };
+    // prologue: pending dt growth, coefficient table for the attempt's dt
+    timed(K_DECIDE, [&]() { return Launch<T>::coef(d, ninst, accurate, s, raw ? 1 : 0); });
     switch (method) {
         case M_ETD2:
             X(XY_NONLIN, R_STATE, 1);
@@ -241,23 +258,26 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             X(XY_REDUCE_FULL, R_CAND);
             break;
     }
-    timed(K_DECIDE, [&]() {
-        cudaError_t q = Launch<T>::decide(d, ninst, raw ? 1 : 0, s);
-        return q == cudaSuccess ? Launch<T>::coef(d, ninst, accurate, s) : q;
-    });
+    timed(K_DECIDE, [&]() { return Launch<T>::decide(d, ninst, raw ? 1 : 0, s); });
     return r;
 }
 
+// Arena of one instance.  Stepped-state spectra (phi-hat x2, a-hat) hold 16
+// bytes per mode in both forms (FP64 complex, or FP32 double-float pairs);
+// every other field is one complex T per mode.
 template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* layout = nullptr) {
-    const size_t ns = (size_t)p.nz * p.ny * p.nc * sizeof(T) * 2;
+    const size_t ns = (size_t)p.nz * p.ny * p.nc;
     const int ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const int nfields = 12 + (p.method == M_ETD4 ? 2 : 0);
+    const size_t fs = al(ns * 16), fp = al(ns * sizeof(T) * 2);
+    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0);  // Nu, P x6, A, B (+ Na, Nb)
     size_t off = 0;
     if (layout) layout[0] = off;
-    off += al(ns) * nfields;
+    off += 3 * fs;
+    if (layout) layout[6] = off;
+    off += nplain * fp;
     if (layout) layout[1] = off;
-    off += al((size_t)(p.kmax + 1) * 8 * sizeof(T));
+    off += al((size_t)kNTab * (p.kmax + 1) * 8 * sizeof(T));
     if (layout) layout[2] = off;
     off += al((size_t)p.nz * 4 * sizeof(double));
     if (layout) layout[3] = off;
@@ -292,7 +312,7 @@ template <class T> class Stepper final : public Handle {
                         sizeof(T) == 4 ? "FP32" : "FP64");
         ns = (size_t)p.nz * p.ny * p.nc;
         ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
-        size_t lay[6];
+        size_t lay[7];
         arena_bytes = instance_arena_bytes<T>(p, lay);
         CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
@@ -301,11 +321,14 @@ template <class T> class Stepper final : public Handle {
         }
         CB_CK(cudaMemsetAsync(arena, 0, arena_bytes, st));
         char* base = (char*)arena;
-        const size_t fb = ((ns * sizeof(T) * 2) + 255) & ~(size_t)255;
-        void** f[14] = {&h.spec[0], &h.spec[1], &h.ahat, &h.Nu, &h.P[0][0], &h.P[0][1], &h.P[1][0], &h.P[1][1],
-                        &h.P[2][0], &h.P[2][1], &h.A, &h.B, &h.Na, &h.Nb};
-        const int nfields = 12 + (p.method == M_ETD4 ? 2 : 0);
-        for (int i = 0; i < nfields; ++i) *f[i] = base + lay[0] + i * fb;
+        const size_t fs = ((ns * 16) + 255) & ~(size_t)255;
+        const size_t fp = ((ns * sizeof(T) * 2) + 255) & ~(size_t)255;
+        void** fst[3] = {&h.spec[0], &h.spec[1], &h.ahat};
+        for (int i = 0; i < 3; ++i) *fst[i] = base + lay[0] + i * fs;
+        void** f[11] = {&h.Nu, &h.P[0][0], &h.P[0][1], &h.P[1][0], &h.P[1][1], &h.P[2][0], &h.P[2][1],
+                        &h.A, &h.B, &h.Na, &h.Nb};
+        const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0);
+        for (int i = 0; i < nplain; ++i) *f[i] = base + lay[6] + i * fp;
         h.coef = reinterpret_cast<T*>(base + lay[1]);
         h.part_xy = reinterpret_cast<double*>(base + lay[2]);
         h.part_z = reinterpret_cast<double*>(base + lay[3]);
@@ -328,6 +351,34 @@ template <class T> class Stepper final : public Handle {
 
     long long bytes() const override { return (long long)arena_bytes; }
 
+    // ---- used by the batched / served pools (pool.cu)
+    const InstT<T>& inst() const { return h; }
+    const Params& params() const { return p; }
+    int accurate() const { return e.accurate; }
+    int tiles() const { return ntiles; }
+    // arm the device loop state for `nsteps` more accepted steps (as run() does)
+    int prepare_run(int nsteps) {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        CB_CK(pull());
+        hc.target = hc.steps + nsteps;
+        hc.done = nsteps == 0 ? 1 : 0;
+        hc.status = nsteps == 0 ? ST_TARGET : ST_RUNNING;
+        CB_CK(push());
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+    // after a pooled run: record the exit reason and leave the instance live
+    int finish_run(int* status) {
+        CB_CK(pull());
+        last_status = hc.status;
+        if (status) *status = hc.status;
+        hc.done = 0;
+        CB_CK(push());
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
     // phi staging buffer: the two work partials are contiguous in the arena and
     // hold at least N doubles; A is the transform intermediate.  Both are
     // free between attempts, so set/get_phi allocate nothing.
@@ -341,7 +392,7 @@ template <class T> class Stepper final : public Handle {
         }
         reset_ctrl();
         CB_CK(push());
-        CB_CK(fwd3d(src, h.spec[0], h.A));
+        CB_CK(fwd3d(src, h.spec[0], h.A, true));
         CB_CK(zpass(Z_INV_STATE, R_STATE));
         CB_CK(xypass(XY_REDUCE_FULL, R_STATE));
         CB_CK(pull());
@@ -359,10 +410,10 @@ template <class T> class Stepper final : public Handle {
         const double ve = s.V - hc.alpha, se = s.S - hc.beta;
         s.E = p.eta * s.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
         hc.E_state = hc.E_init = s.E;
+        hc.grow_pending = p.adaptive ? 1 : 0;  // the loop grows dt before its first step
         CB_CK(push());
         CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
         have_state = true;
-        grown0 = false;
         CB_CK(cudaStreamSynchronize(st));
         return CB_OK;
     }
@@ -371,7 +422,7 @@ template <class T> class Stepper final : public Handle {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         CB_CK(pull());
         double* dst = dev ? out : stage();
-        CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A));
+        CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A, true));
         if (!dev) CB_CK(cudaMemcpyAsync(out, stage(), (size_t)p.N * sizeof(double), cudaMemcpyDeviceToHost, st));
         CB_CK(cudaStreamSynchronize(st));
         return CB_OK;
@@ -395,6 +446,7 @@ template <class T> class Stepper final : public Handle {
         s->attempts = hc.attempts;
         s->rejects = hc.rejects;
         s->status = last_status;
+        s->E_attempt = hc.E_last_attempt;
         return CB_OK;
     }
 
@@ -436,10 +488,6 @@ template <class T> class Stepper final : public Handle {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         if (nsteps < 0) return fail(CB_EINVAL, "nsteps < 0");
         CB_CK(pull());
-        if (p.adaptive && !grown0 && hc.steps % p.grow_every == 0) {  // first step's growth
-            hc.dt = (hc.dt * p.cap_probe < p.dt_cap) ? hc.dt * p.grow_factor : p.dt_cap;
-        }
-        grown0 = true;
         const int steps0 = hc.steps, att0 = hc.attempts;
         hc.target = hc.steps + nsteps;
         hc.done = nsteps == 0 ? 1 : 0;
@@ -509,20 +557,20 @@ template <class T> class Stepper final : public Handle {
         }
         const void* phat = h.spec[hc.spec_state];
         double* phi = rbuf[0];
-        auto need_phi = [&]() { return inv3d(phat, SM_NONE, phi); };
+        auto need_phi = [&]() { return inv3d(phat, SM_NONE, phi, nullptr, true); };
         const double eps = p.eps;
         switch (which) {
-            case CB_FIELD_PHI: CB_CK(inv3d(phat, SM_NONE, dst)); break;
-            case CB_FIELD_FD: CB_CK(Launch<T>::to_double(phat, dst, ns, st)); break;
-            case CB_FIELD_LAP: CB_CK(inv3d(phat, SM_LAP, dst)); break;
-            case CB_FIELD_DX: CB_CK(inv3d(phat, SM_DX, dst)); break;
-            case CB_FIELD_DY: CB_CK(inv3d(phat, SM_DY, dst)); break;
-            case CB_FIELD_DZ: CB_CK(inv3d(phat, SM_DZ, dst)); break;
+            case CB_FIELD_PHI: CB_CK(inv3d(phat, SM_NONE, dst, nullptr, true)); break;
+            case CB_FIELD_FD: CB_CK(Launch<T>::state_to_double(phat, dst, ns, st)); break;
+            case CB_FIELD_LAP: CB_CK(inv3d(phat, SM_LAP, dst, nullptr, true)); break;
+            case CB_FIELD_DX: CB_CK(inv3d(phat, SM_DX, dst, nullptr, true)); break;
+            case CB_FIELD_DY: CB_CK(inv3d(phat, SM_DY, dst, nullptr, true)); break;
+            case CB_FIELD_DZ: CB_CK(inv3d(phat, SM_DZ, dst, nullptr, true)); break;
             case CB_FIELD_F:
             case CB_FIELD_G0:
             case CB_FIELD_NLD: {
                 CB_CK(need_phi());
-                CB_CK(inv3d(phat, SM_LAP, rbuf[1]));
+                CB_CK(inv3d(phat, SM_LAP, rbuf[1], nullptr, true));
                 double* f = which == CB_FIELD_F ? dst : rbuf[2];
                 CB_CK(launch_pointwise(0, N, f, phi, rbuf[1], nullptr, nullptr, eps, 0, 0, 0, st));
                 if (which == CB_FIELD_G0) {  // Calc.cu:171-188: g0 = -lap f + (3 phi^2 - 1) f / eps^2
@@ -539,9 +587,9 @@ template <class T> class Stepper final : public Handle {
             }
             case CB_FIELD_S: {  // Calc.cu:358-374
                 CB_CK(need_phi());
-                CB_CK(inv3d(phat, SM_DX, rbuf[1]));
-                CB_CK(inv3d(phat, SM_DY, rbuf[2]));
-                CB_CK(inv3d(phat, SM_DZ, rbuf[3]));
+                CB_CK(inv3d(phat, SM_DX, rbuf[1], nullptr, true));
+                CB_CK(inv3d(phat, SM_DY, rbuf[2], nullptr, true));
+                CB_CK(inv3d(phat, SM_DZ, rbuf[3], nullptr, true));
                 CB_CK(launch_pointwise(4, N, dst, phi, rbuf[1], rbuf[2], rbuf[3], eps, 0, 0, 0, st));
                 break;
             }
@@ -575,9 +623,6 @@ template <class T> class Stepper final : public Handle {
     int run_timed(int nsteps, long long flush_bytes, double* ms_out, int* att_out) override {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         CB_CK(pull());
-        if (p.adaptive && !grown0 && hc.steps % p.grow_every == 0)
-            hc.dt = (hc.dt * p.cap_probe < p.dt_cap) ? hc.dt * p.grow_factor : p.dt_cap;
-        grown0 = true;
         hc.target = hc.steps + nsteps;
         hc.done = nsteps == 0 ? 1 : 0;
         hc.status = ST_RUNNING;
@@ -672,6 +717,7 @@ template <class T> class Stepper final : public Handle {
         c.beta = up.beta;
         c.fresh = 1;
         c.target = INT_MAX;
+        c.fill_slot = -1;
         hc = c;
         last_status = ST_RUNNING;
     }
@@ -697,7 +743,7 @@ template <class T> class Stepper final : public Handle {
         return Launch<T>::z(p.nz, d, 1, ntiles, a, st);
     }
     // real double field -> spectrum (x 1/N), through the partial buffer `part`
-    cudaError_t fwd3d(const double* src, void* spec, void* part = nullptr) {
+    cudaError_t fwd3d(const double* src, void* spec, void* part = nullptr, bool to_state = false) {
         if (!part) part = tmpP;
         XYArgs a;
         memset(&a, 0, sizeof a);
@@ -709,17 +755,19 @@ template <class T> class Stepper final : public Handle {
         ZArgs z;
         memset(&z, 0, sizeof z);
         z.mode = Z_FWD_PLAIN;
+        z.state_io = to_state ? IO_COUT_STATE : 0;
         z.cin = part;
         z.cout = spec;
         return Launch<T>::z(p.nz, d, 1, ntiles, z, st);
     }
     // spectrum (x multiplier) -> real double field, through `part`
-    cudaError_t inv3d(const void* spec, int mul, double* dst, void* part = nullptr) {
+    cudaError_t inv3d(const void* spec, int mul, double* dst, void* part = nullptr, bool from_state = false) {
         if (!part) part = tmpP;
         ZArgs z;
         memset(&z, 0, sizeof z);
         z.mode = Z_INV_PLAIN;
         z.mul = mul;
+        z.state_io = from_state ? IO_CIN_STATE : 0;
         z.cin = spec;
         z.cout = part;
         cudaError_t r = Launch<T>::z(p.nz, d, 1, ntiles, z, st);
@@ -786,7 +834,7 @@ template <class T> class Stepper final : public Handle {
     cudaGraphExec_t g_loop = nullptr, g_raw = nullptr;
     void* flush_buf = nullptr;
     long long flush_size = 0;
-    bool have_state = false, grown0 = false;
+    bool have_state = false;
     int last_status = ST_RUNNING;
 };
 

@@ -28,18 +28,13 @@ template <class T> struct Acc;
 template <> struct Acc<double> {
     double s = 0.0;
     __device__ __forceinline__ void add(double x) { s += x; }
-    __device__ __forceinline__ double get() const { return s; }
+    __device__ __forceinline__ double part() const { return s; }
 };
-// FP32 values summed with Kahan compensation, handed to FP64 at the end
+// FP32 values summed as a double-float pair (error-free TwoSum per add)
 template <> struct Acc<float> {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        float y = x - c;
-        float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+    FF v{0.f, 0.f};
+    __device__ __forceinline__ void add(float x) { v = ff_add(v, FF{x, 0.f}); }
+    __device__ __forceinline__ FF part() const { return v; }
 };
 
 __device__ __forceinline__ int part_set(const Ctrl* ctrl, int role) {
@@ -57,9 +52,9 @@ __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* pa
     }
     Scal& s = ctrl->sc[role];
     const double c3 = 3.0 / (2.0 * sqrt(2.0));
-    s.sum_u = su;
+    (void)su;  // V comes from the exact k = 0 mode the z pass stored in sum_u
     s.sum_s2 = ss;
-    s.V = (su * p.invN + 1.0) * 0.5 * p.L3;
+    s.V = (s.sum_u * p.invN + 1.0) * 0.5 * p.L3;
     s.S = (0.5 * p.eps * s.grad2 + 0.25 / p.eps * (ss * p.invN)) * c3 * p.L3;
     if (full) {
         s.sum_f2 = sf;
@@ -99,7 +94,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         for (int i = tid; i < M + NX; i += NT) twM[i] = gx[i];  // twM and twN are contiguous
         for (int i = tid; i < NY; i += NT) twY[i] = gy[i];
     }
-    const T cx = (T)p.cx;
+    const T cx = PC<T>(p).cx;
     const size_t plane = (size_t)NY * NC;
 
     if (a.mode == XY_FWD_PLAIN) {
@@ -189,20 +184,28 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         }
 
         // ---- pointwise over all slots (order-free)
-        const T eps = (T)p.eps, ieps = (T)(1.0 / p.eps), ieps2 = (T)(1.0 / (p.eps * p.eps)),
-                ieps3 = (T)(1.0 / (p.eps * p.eps * p.eps));
+        const PC<T> k(p);
+        const T eps = k.eps, ieps = k.ieps, ieps2 = k.ieps2, ieps3 = k.ieps3;
         if (a.mode == XY_NONLIN) {
-            const Scal& sc = ctrl->sc[a.role];
-            const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
-            const T eta = (T)p.eta;
-            const T kappa = (T)2.0, D = (T)1.5;  // phasefield.cpp:259-260
+            // lambda_1 = M1 (V - alpha), lambda_2 = M2 (S - beta) (belastic.cpp:478-479),
+            // formed once per CTA in FP64 and broadcast in the kernel's precision
+            T* lam = reinterpret_cast<T*>(red);
             const bool euler = p.method == M_EULER;
+            if (tid == 0) {
+                const Scal& sc = ctrl->sc[a.role];
+                const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
+                lam[0] = euler ? (T)(0.5 * lam1) : (T)(-0.5 * lam1);
+                lam[1] = euler ? (T)lam2 : (T)(-lam2 * 1.0606601717798212866);  // 3 / (2 sqrt 2)
+            }
+            __syncthreads();
+            const T eta = k.eta;
+            const T kappa = (T)2.0, D = (T)1.5;  // phasefield.cpp:259-260
             // ETD  (Calc.cu:428-437 with nld from :265-284):
             //   G = -lam1/2 - c3 lam2 f - eta (D t / eps^3 + (3u^2 - D - 1) f / eps^2),  H = t
             // Euler (Calc.cu:410-419 with g0 from :171-180):
             //   G = lam1/2 + lam2 f + eta (3u^2 - 1) f / eps^2,                         H = f
-            const T g_c = euler ? (T)(0.5 * lam1) : (T)(-0.5 * lam1);
-            const T g_f = euler ? (T)lam2 : (T)(-lam2 * 3.0 / (2.0 * sqrt(2.0)));
+            const T g_c = lam[0];
+            const T g_f = lam[1];
             for (int it = tid; it < NY * M; it += NT) {
                 const int q = it % M, r = it / M;
                 C* pu = S + r * pitch + q;
@@ -248,8 +251,10 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                     }
                 }
             }
-            double v[3] = {au.get(), as.get(), af.get()};
-            block_sum<3>(v, red);
+            auto pv = au.part();
+            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            double v[3];
+            block_sum<3>(vv, v, red);
             double* part = I.part_xy;
             if (tid == 0) {
                 part[4 * z + 0] = v[0];
@@ -307,7 +312,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     } else {
         outA = reinterpret_cast<C*>(a.cout) + (size_t)z * plane;
     }
-    const T bnl = (T)((p.method == M_EULER) ? p.eta : -p.eta / p.eps) * cx;
+    const T bnl = PC<T>(p).bnl;
     for (int it = tid; it < NY * M; it += NT) {
         const int c = it % M, ky = it / M;
         const C zg = S[ky * pitch + c];

@@ -23,6 +23,89 @@ template <class T> __device__ __forceinline__ const void* spec_of(const InstT<T>
     return role == R_STATE ? I.spec[c->spec_state] : I.spec[1 - c->spec_state];
 }
 
+// ---- stepped state values.  The plain FP64 form keeps the state in FP64.
+// The FP32 form keeps it as double-float pairs (hi + lo, ~48-bit mantissa):
+// rounding the state itself to FP32 every step injects noise into the weakly
+// damped low-|k| modes that the energy sees at first order (a ~1e-6
+// relative energy drift over a few hundred steps), while the increments the
+// nonlinear term contributes tolerate FP32.  Updates are
+//   next = base (+) (em * base_hi + incr),   em = exp(hL) - 1 from an accurate table,
+// with the (+) done in error-free FP32 arithmetic (TwoSum / FastTwoSum).
+template <class T> struct State;
+template <> struct State<double> {
+    double2 v;
+    __device__ __forceinline__ static State load(const void* p, size_t g) {
+        State s;
+        s.v = reinterpret_cast<const double2*>(p)[g];
+        return s;
+    }
+    __device__ __forceinline__ static State from(double2 w) { State s; s.v = w; return s; }
+    __device__ __forceinline__ void store(void* p, size_t g) const { reinterpret_cast<double2*>(p)[g] = v; }
+    __device__ __forceinline__ double2 work() const { return v; }
+    __device__ __forceinline__ double re_exact() const { return v.x; }
+    // e * base + incr (the reference's own form, Calc.cu:453-455)
+    __device__ __forceinline__ State axpy(double e, double2 incr) const {
+        return from(make_double2(e * v.x + incr.x, e * v.y + incr.y));
+    }
+    __device__ __forceinline__ State add(double2 incr) const {
+        return from(make_double2(v.x + incr.x, v.y + incr.y));
+    }
+    template <class A> __device__ __forceinline__ void norm2_into(A& big, A& small, double w) const {
+        big.add(w * (v.x * v.x + v.y * v.y));
+    }
+};
+
+__device__ __forceinline__ void df_add(float& h, float& l, float d) {
+    const float s = h + d;
+    const float bp = s - h;
+    float e = (h - (s - bp)) + (d - bp);  // TwoSum(h, d)
+    e += l;
+    h = s + e;                           // FastTwoSum(s, e)
+    l = e - (h - s);
+}
+template <> struct State<float> {
+    float2 hi, lo;
+    __device__ __forceinline__ static State load(const void* p, size_t g) {
+        const float4 q = reinterpret_cast<const float4*>(p)[g];
+        State s;
+        s.hi = make_float2(q.x, q.y);
+        s.lo = make_float2(q.z, q.w);
+        return s;
+    }
+    __device__ __forceinline__ static State from(float2 w) {
+        State s;
+        s.hi = w;
+        s.lo = make_float2(0.f, 0.f);
+        return s;
+    }
+    __device__ __forceinline__ void store(void* p, size_t g) const {
+        reinterpret_cast<float4*>(p)[g] = make_float4(hi.x, hi.y, lo.x, lo.y);
+    }
+    __device__ __forceinline__ float2 work() const { return make_float2(hi.x + lo.x, hi.y + lo.y); }
+    __device__ __forceinline__ double re_exact() const { return (double)hi.x + (double)lo.x; }
+    // base (+) (em * base_hi + incr)
+    __device__ __forceinline__ State axpy(float em, float2 incr) const {
+        State r = *this;
+        df_add(r.hi.x, r.lo.x, fmaf(em, hi.x, incr.x));
+        df_add(r.hi.y, r.lo.y, fmaf(em, hi.y, incr.y));
+        return r;
+    }
+    __device__ __forceinline__ State add(float2 incr) const {
+        State r = *this;
+        df_add(r.hi.x, r.lo.x, incr.x);
+        df_add(r.hi.y, r.lo.y, incr.y);
+        return r;
+    }
+    // w |u|^2 with u = hi + lo: hi^2 exactly via FMA, the rest in a second sum
+    template <class A> __device__ __forceinline__ void norm2_into(A& big, A& small, float w) const {
+        const float px = hi.x * hi.x, py = hi.y * hi.y;
+        const float ex = fmaf(hi.x, hi.x, -px), ey = fmaf(hi.y, hi.y, -py);
+        big.add(w * px);
+        big.add(w * py);
+        small.add(w * (ex + ey + 2.f * (hi.x * lo.x + hi.y * lo.y)));
+    }
+};
+
 template <class T, int NZ, int TX, int NT>
 __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
     using C = cplx<T>;
@@ -67,33 +150,40 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
         __syncthreads();
     }
 
-    const T cx = (T)p.cx;
-    const T invN = (T)p.invN;
-    const T bnl = (T)((p.method == M_EULER) ? p.eta : -p.eta / p.eps) * cx;
+    const PC<T> k(p);
+    const T cx = k.cx;
+    const T invN = k.invN;
+    const T bnl = k.bnl;
 
     if (a.mode == Z_FWD_PLAIN) {
         C* out = reinterpret_cast<C*>(a.cout);
+        const bool to_state = (a.state_io & IO_COUT_STATE) != 0;
         for (int it = tid; it < NZ * TX; it += NT) {
             const int c = it % TX, r = it / TX, m = m0 + c;
             if (m >= Mc) continue;
             const int kz = tidx<NZ>(r);
             const C v = S[r * W + c];
-            out[(size_t)kz * Mc + m] = cmk<C>(v.x * invN, v.y * invN);
+            const C o = cmk<C>(v.x * invN, v.y * invN);
+            if (to_state) State<T>::from(o).store(a.cout, (size_t)kz * Mc + m);
+            else out[(size_t)kz * Mc + m] = o;
         }
         return;
     }
 
     // ---- combine: slot r holds kz = tidx(r)
-    const C* phat = reinterpret_cast<const C*>(spec_of(I, ctrl, R_STATE));
-    C* cand = reinterpret_cast<C*>(const_cast<void*>(spec_of(I, ctrl, R_CAND)));
+    const void* phat = spec_of(I, ctrl, R_STATE);
+    void* cand = const_cast<void*>(spec_of(I, ctrl, R_CAND));
     C* Nu = reinterpret_cast<C*>(I.Nu);
     C* Na = reinterpret_cast<C*>(I.Na);
     C* Nb = reinterpret_cast<C*>(I.Nb);
-    C* ah = reinterpret_cast<C*>(I.ahat);
-    const T* coef = I.coef;
-    const T dtga = (T)(ctrl->dt * p.ga);
+    void* ah = I.ahat;
+    const T* coef = I.coef + (size_t)ctrl->tab_cur * (size_t)(p.kmax + 1) * 8;
+    T* bc = reinterpret_cast<T*>(red);  // dt * ga, formed once per CTA
+    if (tid == 0) bc[0] = (T)(ctrl->dt * p.ga);
+    __syncthreads();
+    const T dtga = bc[0];
     const bool ref4 = p.etd4_ref != 0;
-    Acc<T> ag, al;
+    Acc<T> ag, ag2, al;
     for (int it = tid; it < NZ * TX; it += NT) {
         const int c = it % TX, r = it / TX, m = m0 + c;
         if (m >= Mc) {
@@ -113,68 +203,65 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             nh = cmk<C>((va.x + mz * vb.x) * invN, (va.y + mz * vb.y) * invN);
         }
         const T* cf = coef + 8 * (kx * kx + kyf * kyf + kzf * kzf);
+        State<T> us;           // the new stage / state spectrum
+        bool have_state = true;
         C un;
         switch (a.mode) {
-            case Z_ETD2_S1: {
+            case Z_ETD2_S1: {  // a = e phi + c1 N_u (Calc.cu:453-455)
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
-                const T e1 = cf[0], c1 = cf[1];
-                const C ph = phat[g];
-                un = cmk<C>(e1 * ph.x + c1 * nh.x, e1 * ph.y + c1 * nh.y);
-                ah[g] = un;
+                us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
+                us.store(ah, g);
                 break;
             }
-            case Z_ETD2_S2: {
-                const T c2 = cf[2];
-                const C av = ah[g], nu = Nu[g];
-                un = cmk<C>(av.x + c2 * (nh.x - nu.x), av.y + c2 * (nh.y - nu.y));
-                cand[g] = un;
+            case Z_ETD2_S2: {  // phi' = a + c2 (N_a - N_u) (Calc.cu:476-477)
+                const C nu = Nu[g];
+                us = State<T>::load(ah, g).add(cmk<C>(cf[2] * (nh.x - nu.x), cf[2] * (nh.y - nu.y)));
+                us.store(cand, g);
                 break;
             }
-            case Z_ETD4_S1: {
+            case Z_ETD4_S1: {  // a = e_h phi + c_h N_u (Calc.cu:495-497)
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
-                const T eh = cf[0], ch = cf[1];
-                const C ph = phat[g];
-                un = cmk<C>(eh * ph.x + ch * nh.x, eh * ph.y + ch * nh.y);
-                ah[g] = un;
+                us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
+                us.store(ah, g);
                 break;
             }
-            case Z_ETD4_S2: {
+            case Z_ETD4_S2: {  // b = e_h phi + c_h N_a (Calc.cu:516-518)
                 Na[g] = nh;
-                const T eh = cf[0], ch = cf[1];
-                const C ph = phat[g];
-                un = cmk<C>(eh * ph.x + ch * nh.x, eh * ph.y + ch * nh.y);
+                us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                 break;
             }
-            case Z_ETD4_S3: {
+            case Z_ETD4_S3: {  // c = e_h a + c_h (2 N_b - N_u) (Calc.cu:537-538)
                 Nb[g] = nh;
-                const T eh = cf[0], ch = cf[1];
-                const C av = ah[g], nu = Nu[g];
-                un = cmk<C>(eh * av.x + ch * ((T)2 * nh.x - nu.x), eh * av.y + ch * ((T)2 * nh.y - nu.y));
+                const C nu = Nu[g];
+                us = State<T>::load(ah, g).axpy(
+                    cf[0], cmk<C>(cf[1] * ((T)2 * nh.x - nu.x), cf[1] * ((T)2 * nh.y - nu.y)));
                 break;
             }
-            case Z_ETD4_S4: {
-                const T e2 = cf[2], f1 = cf[3], f2 = cf[4], f3 = cf[5];
-                const C ph = phat[g], n1 = ref4 ? Na[g] : Nu[g], nb = Nb[g];
-                un = cmk<C>(e2 * ph.x + f1 * n1.x + f2 * (n1.x + nb.x) + f3 * nh.x,
-                            e2 * ph.y + f1 * n1.y + f2 * (n1.y + nb.y) + f3 * nh.y);
-                cand[g] = un;
+            case Z_ETD4_S4: {  // e2 phi + f1 N1 + f2 (N1 + N_b) + f3 N_c (Calc.cu:556-567)
+                const T f1 = cf[3], f2 = cf[4], f3 = cf[5];
+                const C n1 = ref4 ? Na[g] : Nu[g], nb = Nb[g];
+                const C inc = cmk<C>(f1 * n1.x + f2 * (n1.x + nb.x) + f3 * nh.x,
+                                     f1 * n1.y + f2 * (n1.y + nb.y) + f3 * nh.y);
+                us = State<T>::load(phat, g).axpy(cf[2], inc);
+                us.store(cand, g);
                 break;
             }
-            case Z_EULER: {
+            case Z_EULER: {  // phi' = phi - dt ga R (Calc.cu:393-402)
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
-                const C ph = phat[g];
-                un = cmk<C>(ph.x - dtga * nh.x, ph.y - dtga * nh.y);
-                cand[g] = un;
+                us = State<T>::load(phat, g).add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
+                us.store(cand, g);
                 const T wgt = (kx == 0 || 2 * kx == nx) ? (T)1 : (T)2;
                 al.add(wgt * (nh.x * nh.x + nh.y * nh.y));
                 break;
             }
             case Z_INV_STATE: {
-                un = reinterpret_cast<const C*>(spec_of(I, ctrl, a.role))[g];
+                us = State<T>::load(spec_of(I, ctrl, a.role), g);
                 break;
             }
             default: {  // Z_INV_PLAIN with an optional spectral multiplier
-                const C v = reinterpret_cast<const C*>(a.cin)[g];
+                have_state = false;
+                const C v = (a.state_io & IO_CIN_STATE) ? State<T>::load(a.cin, g).work()
+                                                        : reinterpret_cast<const C*>(a.cin)[g];
                 if (a.mul == SM_LAP) {
                     const T mm = -cx * (T)(kx * kx + kyf * kyf + kzf * kzf);
                     un = cmk<C>(mm * v.x, mm * v.y);
@@ -192,13 +279,17 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
                 break;
             }
         }
-        if (a.mode != Z_INV_PLAIN) {
+        if (have_state) {
+            un = us.work();
             // Parseval: mean |grad u|^2 = sum over the full spectrum of |k_g|^2 |u-hat|^2
+            // (cx applied once, in FP64, when the sums are finalised)
             const int gx = (2 * kx == nx) ? 0 : kx;
             const int gy = (2 * ky == ny) ? 0 : kyf;
             const int gz = (2 * kz == NZ) ? 0 : kzf;
-            const T wgt = (kx == 0 || 2 * kx == nx) ? (T)1 : (T)2;
-            ag.add(wgt * cx * (T)(gx * gx + gy * gy + gz * gz) * (un.x * un.x + un.y * un.y));
+            const T wgt = ((kx == 0 || 2 * kx == nx) ? (T)1 : (T)2) * (T)(gx * gx + gy * gy + gz * gz);
+            if (wgt != (T)0) us.norm2_into(ag, ag2, wgt);
+            // volume from the k = 0 mode: mean u = Re u-hat(0), exactly
+            if (m == 0 && kz == 0) ctrl->sc[a.role].sum_u = us.re_exact() * (double)p.N;
         }
         const T mz = -cx * (T)(kzf * kzf);
         S[r * W + c] = un;
@@ -227,8 +318,13 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
     }
     if (a.mode == Z_INV_PLAIN) return;
 
-    double v[2] = {ag.get(), al.get()};
-    block_sum<2>(v, red);
+    auto g0 = ag.part();
+    if constexpr (sizeof(T) == 4) g0 = ff_add(g0, ag2.part());
+    else g0 += ag2.part();
+    decltype(g0) vv[2] = {g0, al.part()};
+    double v[2];
+    __syncthreads();  // red held dt*ga
+    block_sum<2>(vv, v, red);
     if (tid == 0) {
         double* part = I.part_z;
         part[2 * blockIdx.x + 0] = v[0];
@@ -242,7 +338,7 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
                 s0 += __ldcg(part + 2 * b);
                 s1 += __ldcg(part + 2 * b + 1);
             }
-            ctrl->sc[a.role].grad2 = s0;
+            ctrl->sc[a.role].grad2 = s0 * p.cx;
             if (a.mode == Z_EULER) ctrl->sc[a.role].lsq = s1;
             ctrl->cnt_z[a.role] = 0u;
         }

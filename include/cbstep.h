@@ -101,6 +101,7 @@ typedef struct cb_scalars {
     double dt, t;
     double lserror;          /* Euler LSerror of the last step (belastic.cpp:414) */
     int steps, attempts, rejects, status;
+    double E_attempt;        /* energy of the last attempted candidate (accepted or not) */
 } cb_scalars;
 
 typedef struct cb_run_stats {
@@ -158,6 +159,58 @@ long long cb_handle_bytes(cb_handle* h);
  * 3 z pass, 4 decide + coefficient table. */
 int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts);
 int cb_profile_kernels(cb_handle* h, int nattempts, long long flush_bytes, double* ms, int* counts);
+
+/* ---- batched vesicles (no counterpart in the reference, which runs one grid
+ * per process, main.cpp:17-18).  Instances of uneven grids advance together:
+ * one launch per pass covers every instance of a grid size, and one CUDA
+ * graph runs an attempt of every instance.  Each instance keeps its own dt,
+ * accept/reject state and exit test.  All instances share one precision. */
+typedef struct cb_batch cb_batch;
+int cb_batch_create(const cb_params* params, int n, cb_batch** out);
+int cb_batch_destroy(cb_batch* b);
+int cb_batch_set_phi(cb_batch* b, int i, const double* phi, int on_device);
+int cb_batch_get_phi(cb_batch* b, int i, double* phi, int on_device);
+int cb_batch_scalars(cb_batch* b, int i, cb_scalars* s);
+/* every instance takes nsteps more accepted steps (or stops at its own exit test) */
+int cb_batch_run(cb_batch* b, int nsteps, cb_run_stats* st);
+/* same, one attempt per CUDA-event pair with an L2 flush of flush_bytes between */
+int cb_batch_run_timed(cb_batch* b, int nsteps, long long flush_bytes, double* device_ms, cb_run_stats* st);
+
+/* ---- served relaxations (no counterpart in the reference).  A request is a
+ * relaxation of a seeded ellipsoid phi0 = tanh(d / (sqrt(2) eps)) until an
+ * accepted step changes E by less than params.rel_tol |E| (CB_DONE_CONVERGED)
+ * or max_steps accepted steps pass (CB_DONE_TARGET: not converged).
+ * cb_serve_trace replays an arrival trace in real time with continuous
+ * batching: arrivals queue FIFO, the head is admitted while its grid class has
+ * a free slot and hbm_budget_bytes holds its state, admitted requests advance
+ * together `quantum` attempts at a time and leave as soon as they finish. */
+typedef struct cb_request {
+    cb_params params;
+    double axes[3], centre[3];    /* ellipsoid semi-axes and centre */
+    double axes2[3], centre2[3];  /* optional second ellipsoid (union) when axes2[0] > 0 */
+    double arrival_s;             /* arrival time from the start of the trace */
+    int max_steps;
+    int pad;
+} cb_request;
+
+typedef struct cb_result {
+    double arrival_s, admitted_s, finished_s, latency_s;
+    double E, V, S;
+    int steps, attempts, status, pad;
+    long long bytes;
+} cb_result;
+
+typedef struct cb_serve_stats {
+    double wall_s;
+    double point_steps;       /* sum over requests of grid points x accepted steps */
+    int completed;
+    int graph_launches;
+    long long peak_bytes;     /* largest admitted stepping state */
+} cb_serve_stats;
+
+/* phi_out: NULL, or n pointers (NULL entries skip) that receive each request's final phi */
+int cb_serve_trace(const cb_request* reqs, int n, long long hbm_budget_bytes, int max_slots_per_class, int quantum,
+                   cb_result* results, double** phi_out, cb_serve_stats* stats);
 
 const char* cb_last_error(void);
 const char* cb_version(void);
