@@ -179,17 +179,18 @@ struct LinearLines {
 };
 // two fields side by side in one padded plane: lines [0, n1) are rows of
 // field 0, lines [n1, 2 n1) rows of field 1 (which starts `second` slots in)
+template <int N1, int PITCH, int SECOND>
 struct PairRows {
-    int n1, pitch, second;
     __device__ __forceinline__ int operator()(int l) const {
-        return (l < n1) ? l * pitch : (l - n1) * pitch + second;
+        return (l < N1) ? l * PITCH : (l - N1) * PITCH + SECOND;
     }
 };
 
 // NT: natural in -> transposed out.  Lines l in [0, nlines) at buf + off(l),
 // element stride es.  All NTHR threads of the block call it; caller syncs after.
-template <int L, bool INV, int NTHR, class C, class OFF>
-__device__ __forceinline__ void fft_lines_NT(C* buf, int nlines, OFF off, int es, const C* tw) {
+template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
+__device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* tw) {
+    constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
     const int tid = threadIdx.x;
     if constexpr (R2 == 1) {
@@ -234,12 +235,13 @@ __device__ __forceinline__ void fft_lines_NT(C* buf, int nlines, OFF off, int es
 
 // TN: transposed in -> natural out (input element j = j1 + R1 j2 sits at
 // slot j2 + R2 j1, exactly where an NT transform leaves element j).
-template <int L, bool INV, int NTHR, class C, class OFF>
-__device__ __forceinline__ void fft_lines_TN(C* buf, int nlines, OFF off, int es, const C* tw) {
+template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
+__device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* tw) {
+    constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
     const int tid = threadIdx.x;
     if constexpr (R2 == 1) {
-        fft_lines_NT<L, INV, NTHR, C, OFF>(buf, nlines, off, es, tw);
+        fft_lines_NT<L, INV, NTHR, NLINES, C, OFF>(buf, off, es, tw);
     } else {
     // phase A: for each (line, j1) DFT_R2 over j2 (contiguous block at R2*j1), twiddle W_L^{j1 k2}
     for (int it = tid; it < nlines * R1; it += NTHR) {
@@ -302,6 +304,41 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// Sum of `nparts` FP64 partials (NV interleaved values each, stride NV) by a
+// whole block: strided loads, a warp-shuffle tree, then the per-warp sums.
+// The result is valid in thread 0.  Keeps the dependent FP64 chain short; a
+// single thread walking hundreds of partials dominated the kernels' tails.
+template <int NV>
+__device__ __forceinline__ void block_sum_parts(const double* part, int nparts, double* out, double* red) {
+    double v[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) v[j] += __ldcg(part + (size_t)NV * i + j);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) red[j * 32 + w] = v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < nw; ++k) s += red[j * 32 + k];
+            out[j] = s;
+        }
+    }
+}
+
 // Block-wide sum of NV values (FF pairs or doubles); the FP64 result is valid
 // in thread 0.  `red` must hold 32*NV doubles of shared memory.
 template <int NV, class V>

@@ -11,6 +11,7 @@ namespace cb {
 template <class T> struct Launch {
     static bool xy_supported(int nx);
     static bool z_supported(int nz);
+    static bool xy_plain_supported(int nx);
     static int z_tile();
     static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s);
     static cudaError_t z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s);
@@ -18,6 +19,8 @@ template <class T> struct Launch {
     static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw = 1);
     static cudaError_t to_double(const void* in, double* out, size_t n, cudaStream_t s);
     static cudaError_t state_to_double(const void* in, double* out, size_t n, cudaStream_t s);
+    // complex double spectrum <-> stepped state of precision T (to_state = 1: double -> state)
+    static cudaError_t f64_to_state(const void* in, void* out, size_t n, int to_state, cudaStream_t s);
 };
 
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,

@@ -12,26 +12,34 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 template <class T, int NX> struct XYCfg {
     static constexpr int NT = NX <= 32 ? 128 : (NX <= 64 ? 256 : 512);
-    static constexpr bool ok = xy_smem_bytes<T, NX>(2) <= kMaxSmem;
+    static constexpr bool ok = xy_smem_bytes<T, NX>(2) <= kMaxSmem;   // stepping (two fields)
+    static constexpr bool ok1 = xy_smem_bytes<T, NX>(1) <= kMaxSmem;  // plain transforms (one field)
 };
+
+template <class T, int NX, int NF>
+static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    constexpr int NT = XYCfg<T, NX>::NT;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)xy_smem_bytes<T, NX>(NF));
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    xy_kernel<T, NX, NT, NF><<<dim3(nzmax, ninst), NT, xy_smem_bytes<T, NX>(NF), s>>>(d, a);
+    return cudaGetLastError();
+}
 
 template <class T, int NX>
 static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
-    if constexpr (!XYCfg<T, NX>::ok) {
-        return cudaErrorInvalidValue;
-    } else {
-        constexpr int NT = XYCfg<T, NX>::NT;
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)xy_smem_bytes<T, NX>(2));
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
-        const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
-        xy_kernel<T, NX, NT><<<dim3(nzmax, ninst), NT, xy_smem_bytes<T, NX>(nf), s>>>(d, a);
-        return cudaGetLastError();
+    const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN;
+    if constexpr (XYCfg<T, NX>::ok) {
+        if (two) return xy_go_nf<T, NX, 2>(d, ninst, nzmax, a, s);
     }
+    if constexpr (XYCfg<T, NX>::ok1) {
+        if (!two) return xy_go_nf<T, NX, 1>(d, ninst, nzmax, a, s);
+    }
+    return cudaErrorInvalidValue;
 }
 
 template <class T> constexpr int ztile() { return sizeof(T) == 4 ? 16 : 8; }
@@ -57,6 +65,14 @@ static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a
 template <class T> bool Launch<T>::xy_supported(int nx) {
     switch (nx) {
 #define CASE(n) case n: return XYCfg<T, n>::ok;
+        CB_XY_SIZES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
+template <class T> bool Launch<T>::xy_plain_supported(int nx) {
+    switch (nx) {
+#define CASE(n) case n: return XYCfg<T, n>::ok1;
         CB_XY_SIZES(CASE)
 #undef CASE
         default: return false;
@@ -110,6 +126,13 @@ template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out,
 template <class T> cudaError_t Launch<T>::state_to_double(const void* in, double* out, size_t n, cudaStream_t s) {
     const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     state_to_double_kernel<T><<<blocks, 256, 0, s>>>(in, reinterpret_cast<double2*>(out), n);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_state, cudaStream_t s) {
+    const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    f64_state_kernel<T><<<blocks, 256, 0, s>>>(in, out, n, to_state);
     return cudaGetLastError();
 }
 

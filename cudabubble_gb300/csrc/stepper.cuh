@@ -286,6 +286,8 @@ template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* l
     off += al(sizeof(Ctrl));
     if (layout) layout[5] = off;
     off += al(sizeof(InstT<T>));
+    if (layout) layout[7] = off;
+    off += al(sizeof(InstT<double>));  // FP64 descriptor for exact set/get of phi (FP32 form)
     return off;
 }
 
@@ -312,7 +314,7 @@ template <class T> class Stepper final : public Handle {
                         sizeof(T) == 4 ? "FP32" : "FP64");
         ns = (size_t)p.nz * p.ny * p.nc;
         ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
-        size_t lay[7];
+        size_t lay[8];
         arena_bytes = instance_arena_bytes<T>(p, lay);
         CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
@@ -343,6 +345,23 @@ template <class T> class Stepper final : public Handle {
         if (!h.twz) return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(err));
         h.p = p;
         CB_CK(cudaMemcpyAsync(d, &h, sizeof h, cudaMemcpyHostToDevice, st));
+        if (sizeof(T) == 4 && Launch<double>::xy_plain_supported(p.nx)) {
+            // the FP32 form reads and writes phi through FP64 plain transforms, so
+            // its double-float state starts exact (an FP32 forward FFT of phi0
+            // alone costs ~6e-7 of the energy at 128^3)
+            InstT<double> x;
+            memset(&x, 0, sizeof x);
+            x.ctrl = h.ctrl;
+            x.coef = nullptr;
+            x.p = p;
+            x.twx = twiddle_table<double>(p.nx, 1, &err);
+            x.twy = twiddle_table<double>(p.ny, 0, &err);
+            x.twz = twiddle_table<double>(p.nz, 0, &err);
+            if (!x.twx || !x.twy || !x.twz) return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(err));
+            aux = reinterpret_cast<InstT<double>*>(base + lay[7]);
+            aux_h = x;
+            CB_CK(cudaMemcpyAsync(aux, &aux_h, sizeof aux_h, cudaMemcpyHostToDevice, st));
+        }
         memset(&hc, 0, sizeof hc);
         reset_ctrl();
         CB_CK(push());
@@ -392,7 +411,12 @@ template <class T> class Stepper final : public Handle {
         }
         reset_ctrl();
         CB_CK(push());
-        CB_CK(fwd3d(src, h.spec[0], h.A, true));
+        if (aux) {  // exact spectrum: FP64 transform into the 16 B/mode candidate field, then hi/lo split
+            CB_CK(fwd3d_f64(src, h.spec[1], h.ahat));
+            CB_CK(Launch<T>::f64_to_state(h.spec[1], h.spec[0], ns, 1, st));
+        } else {
+            CB_CK(fwd3d(src, h.spec[0], h.A, true));
+        }
         CB_CK(zpass(Z_INV_STATE, R_STATE));
         CB_CK(xypass(XY_REDUCE_FULL, R_STATE));
         CB_CK(pull());
@@ -422,7 +446,13 @@ template <class T> class Stepper final : public Handle {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         CB_CK(pull());
         double* dst = dev ? out : stage();
-        CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A, true));
+        if (aux) {
+            void* s64 = h.spec[1 - hc.spec_state];  // candidate slot: free between attempts
+            CB_CK(Launch<T>::f64_to_state(h.spec[hc.spec_state], s64, ns, 0, st));
+            CB_CK(inv3d_f64(s64, dst, h.ahat));
+        } else {
+            CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A, true));
+        }
         if (!dev) CB_CK(cudaMemcpyAsync(out, stage(), (size_t)p.N * sizeof(double), cudaMemcpyDeviceToHost, st));
         CB_CK(cudaStreamSynchronize(st));
         return CB_OK;
@@ -760,6 +790,38 @@ template <class T> class Stepper final : public Handle {
         z.cout = spec;
         return Launch<T>::z(p.nz, d, 1, ntiles, z, st);
     }
+    // FP64 plain transforms over the auxiliary descriptor (FP32 form only)
+    cudaError_t fwd3d_f64(const double* src, void* spec64, void* part64) {
+        XYArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = XY_FWD_PLAIN;
+        a.rin = src;
+        a.cout = part64;
+        cudaError_t r = Launch<double>::xy(p.nx, aux, 1, p.nz, a, st);
+        if (r != cudaSuccess) return r;
+        ZArgs z;
+        memset(&z, 0, sizeof z);
+        z.mode = Z_FWD_PLAIN;
+        z.cin = part64;
+        z.cout = spec64;
+        return Launch<double>::z(p.nz, aux, 1, ntiles64(), z, st);
+    }
+    cudaError_t inv3d_f64(const void* spec64, double* dst, void* part64) {
+        ZArgs z;
+        memset(&z, 0, sizeof z);
+        z.mode = Z_INV_PLAIN;
+        z.cin = spec64;
+        z.cout = part64;
+        cudaError_t r = Launch<double>::z(p.nz, aux, 1, ntiles64(), z, st);
+        if (r != cudaSuccess) return r;
+        XYArgs a;
+        memset(&a, 0, sizeof a);
+        a.mode = XY_INV_PLAIN;
+        a.cin = part64;
+        a.rout = dst;
+        return Launch<double>::xy(p.nx, aux, 1, p.nz, a, st);
+    }
+    int ntiles64() const { return (p.ny * p.nc + Launch<double>::z_tile() - 1) / Launch<double>::z_tile(); }
     // spectrum (x multiplier) -> real double field, through `part`
     cudaError_t inv3d(const void* spec, int mul, double* dst, void* part = nullptr, bool from_state = false) {
         if (!part) part = tmpP;
@@ -831,6 +893,8 @@ template <class T> class Stepper final : public Handle {
     size_t ns = 0;
     int ntiles = 0;
     cudaStream_t st = nullptr;
+    InstT<double>* aux = nullptr;  // FP64 descriptor for exact set/get of phi (FP32 form)
+    InstT<double> aux_h{};
     cudaGraphExec_t g_loop = nullptr, g_raw = nullptr;
     void* flush_buf = nullptr;
     long long flush_size = 0;

@@ -41,33 +41,31 @@ __device__ __forceinline__ int part_set(const Ctrl* ctrl, int role) {
     return role == R_WORK ? 2 : (role == R_STATE ? ctrl->part_state : 1 - ctrl->part_state);
 }
 
-// Finalise the FP64 scalars of one state (phasefield.cpp:283-325,
-// belastic.cpp:68-86); run by one thread of the last CTA.
-__device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* part, int role, bool full) {
-    double su = 0.0, ss = 0.0, sf = 0.0;
-    for (int z = 0; z < p.nz; ++z) {
-        su += __ldcg(part + 4 * z + 0);
-        ss += __ldcg(part + 4 * z + 1);
-        sf += __ldcg(part + 4 * z + 2);
-    }
+// Finalise the FP64 scalars of one state from the per-plane sums
+// (phasefield.cpp:283-325, belastic.cpp:68-86); thread 0 of the last CTA.
+__device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* sums, int role, bool full) {
+    const double ss = sums[1], sf = sums[2];
     Scal& s = ctrl->sc[role];
-    const double c3 = 3.0 / (2.0 * sqrt(2.0));
-    (void)su;  // V comes from the exact k = 0 mode the z pass stored in sum_u
+    const double c3 = 1.0606601717798212866;  // 3 / (2 sqrt 2)
+    // V comes from the exact k = 0 mode the z pass stored in sum_u
     s.sum_s2 = ss;
     s.V = (s.sum_u * p.invN + 1.0) * 0.5 * p.L3;
-    s.S = (0.5 * p.eps * s.grad2 + 0.25 / p.eps * (ss * p.invN)) * c3 * p.L3;
+    s.S = (0.5 * p.eps * s.grad2 + 0.25 * p.d_ieps * (ss * p.invN)) * c3 * p.L3;
     if (full) {
         s.sum_f2 = sf;
-        s.E_el = (sf * p.invN) * (1.0 / (p.eps * 2.0)) * p.L3;
+        s.E_el = (sf * p.invN) * (0.5 * p.d_ieps) * p.L3;
         const double ve = s.V - ctrl->alpha, se = s.S - ctrl->beta;
         s.E = p.eta * s.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
     }
 }
 
-template <class T, int NX, int NT>
+// NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN, 1 otherwise
+template <class T, int NX, int NT, int NF>
 __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
     using C = cplx<T>;
     constexpr int M = NX / 2, NY = NX, NC = M + 1;
+    constexpr int nf = NF;
+    constexpr int pitch = nf * M + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
@@ -80,8 +78,6 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         if (ctrl->done) return;
         if (a.skip_if_stale && !ctrl->fresh) return;
     }
-    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
-    const int pitch = nf * M + 1;
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
     C* twM = S + NY * pitch;                // W_M^m
     C* twN = twM + M;                       // W_NX^m
@@ -144,10 +140,10 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         }
         __syncthreads();
         // ---- y inverse (natural in, transposed out) on nf*M columns
-        fft_lines_NT<NY, true, NT>(S, nf * M, LinearLines{1}, pitch, twY);
+        fft_lines_NT<NY, true, NT, nf * M>(S, LinearLines{1}, pitch, twY);
         __syncthreads();
         // ---- x C2R: half-length pre-processing, then inverse M-point FFT per row
-        const PairRows rows{NY, pitch, M};
+        const PairRows<NY, pitch, M> rows;
         for (int it = tid; it < nf * NY * (M / 2 + 1); it += NT) {
             const int l = it % (nf * NY), k = it / (nf * NY);
             C* row = S + rows(l);
@@ -170,7 +166,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             }
         }
         __syncthreads();
-        fft_lines_NT<M, true, NT>(S, nf * NY, rows, 1, twM);
+        fft_lines_NT<M, true, NT, nf * NY>(S, rows, 1, twM);
         __syncthreads();
 
         if (a.mode == XY_INV_PLAIN) {
@@ -256,15 +252,23 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             double v[3];
             block_sum<3>(vv, v, red);
             double* part = I.part_xy;
+            int* last = reinterpret_cast<int*>(red + 128);
             if (tid == 0) {
                 part[4 * z + 0] = v[0];
                 part[4 * z + 1] = v[1];
                 part[4 * z + 2] = v[2];
+                part[4 * z + 3] = 0.0;
                 __threadfence();
                 const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[a.role], 1u);
-                if (done_blocks == (unsigned)(p.nz - 1)) {
-                    __threadfence();
-                    finalize_xy(p, ctrl, part, a.role, full);
+                *last = done_blocks == (unsigned)(p.nz - 1);
+            }
+            __syncthreads();
+            if (*last) {  // the last CTA of this instance finalises, with all its threads
+                __threadfence();
+                double sums[4];
+                block_sum_parts<4>(part, p.nz, sums, red);
+                if (tid == 0) {
+                    finalize_xy(p, ctrl, sums, a.role, full);
                     ctrl->cnt_xy[a.role] = 0u;
                 }
             }
@@ -273,9 +277,9 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     }
 
     // ---- forward xy: x R2C (transposed in, natural out) then y (transposed in, natural out)
-    const int nfo = (a.mode == XY_NONLIN) ? 2 : 1;
-    const PairRows rows{NY, pitch, M};
-    fft_lines_TN<M, false, NT>(S, nfo * NY, rows, 1, twM);
+    constexpr int nfo = NF;  // XY_NONLIN (2 fields) or XY_FWD_PLAIN (1)
+    const PairRows<NY, pitch, M> rows;
+    fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM);
     __syncthreads();
     for (int it = tid; it < nfo * NY * (M / 2 + 1); it += NT) {
         const int l = it % (nfo * NY), k = it / (nfo * NY);
@@ -300,7 +304,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         }
     }
     __syncthreads();
-    fft_lines_TN<NY, false, NT>(S, nfo * M, LinearLines{1}, pitch, twY);
+    fft_lines_TN<NY, false, NT, nfo * M>(S, LinearLines{1}, pitch, twY);
     __syncthreads();
 
     // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
@@ -350,7 +354,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
 }
 
 template <class T, int NX> constexpr size_t xy_smem_bytes(int nf) {
-    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + NX / 2 + NX + NX) + 32 * 4 * sizeof(double);
+    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + NX / 2 + NX + NX) + (32 * 4 + 2) * sizeof(double);
 }
 
 }  // namespace cb

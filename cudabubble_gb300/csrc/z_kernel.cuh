@@ -146,7 +146,8 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             S[zz * W + TX + c] = vb;
         }
         __syncthreads();
-        fft_lines_NT<NZ, false, NT>(S, two ? W : TX, LinearLines{1}, W, tw);
+        if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw);
+        else fft_lines_NT<NZ, false, NT, TX>(S, LinearLines{1}, W, tw);
         __syncthreads();
     }
 
@@ -184,8 +185,15 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
     const T dtga = bc[0];
     const bool ref4 = p.etd4_ref != 0;
     Acc<T> ag, ag2, al;
+    static_assert(NT % TX == 0, "one column per thread");
+    const int c = tid % TX, m = m0 + c;  // fixed column of this thread
+    const int ky = m / nc, kx = m - ky * nc;
+    const int kyf = min(ky, ny - ky);
+    const int kxy = kx * kx + kyf * kyf;
+    const T wxy = (kx == 0 || 2 * kx == nx) ? (T)1 : (T)2;
+    const int gxy = ((2 * kx == nx) ? 0 : kx * kx) + ((2 * ky == ny) ? 0 : kyf * kyf);
     for (int it = tid; it < NZ * TX; it += NT) {
-        const int c = it % TX, r = it / TX, m = m0 + c;
+        const int r = it / TX;
         if (m >= Mc) {
             S[r * W + c] = cmk<C>(0, 0);
             S[r * W + TX + c] = cmk<C>(0, 0);
@@ -193,8 +201,6 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
         }
         const int kz = tidx<NZ>(r);
         const int kzf = min(kz, NZ - kz);
-        const int ky = m / nc, kx = m - ky * nc;
-        const int kyf = min(ky, ny - ky);
         const size_t g = (size_t)kz * Mc + m;
         C nh = cmk<C>(0, 0);
         if (need_fwd) {
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             const T mz = bnl * (T)(kzf * kzf);
             nh = cmk<C>((va.x + mz * vb.x) * invN, (va.y + mz * vb.y) * invN);
         }
-        const T* cf = coef + 8 * (kx * kx + kyf * kyf + kzf * kzf);
+        const T* cf = coef + 8 * (kxy + kzf * kzf);
         State<T> us;           // the new stage / state spectrum
         bool have_state = true;
         C un;
@@ -250,8 +256,7 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
                 us = State<T>::load(phat, g).add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
                 us.store(cand, g);
-                const T wgt = (kx == 0 || 2 * kx == nx) ? (T)1 : (T)2;
-                al.add(wgt * (nh.x * nh.x + nh.y * nh.y));
+                al.add(wxy * (nh.x * nh.x + nh.y * nh.y));
                 break;
             }
             case Z_INV_STATE: {
@@ -283,10 +288,8 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             un = us.work();
             // Parseval: mean |grad u|^2 = sum over the full spectrum of |k_g|^2 |u-hat|^2
             // (cx applied once, in FP64, when the sums are finalised)
-            const int gx = (2 * kx == nx) ? 0 : kx;
-            const int gy = (2 * ky == ny) ? 0 : kyf;
             const int gz = (2 * kz == NZ) ? 0 : kzf;
-            const T wgt = ((kx == 0 || 2 * kx == nx) ? (T)1 : (T)2) * (T)(gx * gx + gy * gy + gz * gz);
+            const T wgt = wxy * (T)(gxy + gz * gz);
             if (wgt != (T)0) us.norm2_into(ag, ag2, wgt);
             // volume from the k = 0 mode: mean u = Re u-hat(0), exactly
             if (m == 0 && kz == 0) ctrl->sc[a.role].sum_u = us.re_exact() * (double)p.N;
@@ -297,7 +300,8 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
     }
     __syncthreads();
     const bool two = a.mode != Z_INV_PLAIN;
-    fft_lines_TN<NZ, true, NT>(S, two ? W : TX, LinearLines{1}, W, tw);
+    if (two) fft_lines_TN<NZ, true, NT, W>(S, LinearLines{1}, W, tw);
+    else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw);
     __syncthreads();
 
     // ---- store partials (natural z)
@@ -325,28 +329,30 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
     double v[2];
     __syncthreads();  // red held dt*ga
     block_sum<2>(vv, v, red);
+    double* part = I.part_z;
+    int* last = reinterpret_cast<int*>(red + 64);
     if (tid == 0) {
-        double* part = I.part_z;
         part[2 * blockIdx.x + 0] = v[0];
         part[2 * blockIdx.x + 1] = v[1];
         __threadfence();
         const unsigned prev = atomicAdd(&ctrl->cnt_z[a.role], 1u);
-        if (prev == (unsigned)(ntiles - 1)) {
-            __threadfence();
-            double s0 = 0.0, s1 = 0.0;
-            for (int b = 0; b < ntiles; ++b) {
-                s0 += __ldcg(part + 2 * b);
-                s1 += __ldcg(part + 2 * b + 1);
-            }
-            ctrl->sc[a.role].grad2 = s0 * p.cx;
-            if (a.mode == Z_EULER) ctrl->sc[a.role].lsq = s1;
+        *last = prev == (unsigned)(ntiles - 1);
+    }
+    __syncthreads();
+    if (*last) {  // the last CTA of this instance finalises, with all its threads
+        __threadfence();
+        double sums[2];
+        block_sum_parts<2>(part, ntiles, sums, red);
+        if (tid == 0) {
+            ctrl->sc[a.role].grad2 = sums[0] * p.cx;
+            if (a.mode == Z_EULER) ctrl->sc[a.role].lsq = sums[1];
             ctrl->cnt_z[a.role] = 0u;
         }
     }
 }
 
 template <class T, int NZ, int TX> constexpr size_t z_smem_bytes() {
-    return sizeof(cplx<T>) * ((size_t)NZ * 2 * TX + NZ) + 32 * 2 * sizeof(double);
+    return sizeof(cplx<T>) * ((size_t)NZ * 2 * TX + NZ) + (32 * 2 + 2) * sizeof(double);
 }
 
 }  // namespace cb
