@@ -20,7 +20,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libcbstep.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "stepper.cu", "pool.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "stepper.cu", "pool.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

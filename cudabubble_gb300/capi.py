@@ -100,6 +100,8 @@ SIGNATURES = {
     "cb_batch_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(cb_run_stats)]),
     "cb_serve_trace": (C.c_int, [_P(cb_request), C.c_int, C.c_longlong, C.c_int, C.c_int, _P(cb_result),
                                  _P(C.c_void_p), _P(cb_serve_stats)]),
+    "cb_intf_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                  C.c_void_p, C.c_void_p]),
     "cb_last_error": (C.c_char_p, []),
     "cb_version": (C.c_char_p, []),
 }

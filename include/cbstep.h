@@ -212,6 +212,21 @@ typedef struct cb_serve_stats {
 int cb_serve_trace(const cb_request* reqs, int n, long long hbm_budget_bytes, int max_slots_per_class, int quantum,
                    cb_result* results, double** phi_out, cb_serve_stats* stats);
 
+/* (mean(u) + addition) * multiply * volume of a device-resident real field
+ * d_u[nz][ny][nx], written to the device double *d_val on `stream` (a
+ * cudaStream_t; NULL is the legacy default stream).  Same quantity as the
+ * reference's Calc::intf (Calc.cu:191-262), but no counterpart there: this
+ * entry point allocates nothing.  Its partial sums live in a fixed file-scope
+ * device array of 4096 planes (32 KiB), so nz > 4096 returns CB_EINVAL; it is
+ * meant for callers that may not allocate device memory at the point of the
+ * call (a carved-up memory pool, a host that forbids allocations after
+ * start-up).  The first call on each device does a synchronous set-up
+ * (resolves the array's address, clears its counter): make it before any
+ * stream capture.  All calls on a device share the one array, so calls that
+ * overlap in time (other streams, other host threads) race; serialise them. */
+int cb_intf_noalloc(const double* d_u, int nx, int ny, int nz, double addition, double multiply, double volume,
+                    double* d_val, void* stream);
+
 const char* cb_last_error(void);
 const char* cb_version(void);
 
