@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <type_traits>
+#include <utility>
 
 namespace cb {
 
@@ -72,6 +73,63 @@ template <class C, bool INV> __device__ __forceinline__ C wconst(int m, int R) {
     return cmk<C>((T)cos2pi(m, R), INV ? (T)sin2pi(m, R) : -(T)sin2pi(m, R));
 }
 
+template <bool INV, class C> __device__ __forceinline__ C tw_get_pre(C w) { return INV ? cconj(w) : w; }
+
+// ------------------------------------------- gain-unbiased FP32 twiddles
+// A twiddle rounded to FP32 has |w| != 1 by up to ~6e-8, and the rounding of
+// a given constant has the same sign every time it is applied: the FP32
+// transforms then carried a systematic gain of ~-6e-9 on the field, which the
+// energy (a near-cancellation of eps lap u and (u^3 - u) / eps) amplified to
+// ~5e-7.  In the FP32 form every twiddle is therefore split w = hi + lo and the
+// product a * w is formed with the lo part folded in before the one rounding,
+// so the only errors left are unbiased roundings.  The FP64 form keeps plain
+// products.
+__device__ __forceinline__ float2 cmul_comp(float2 a, float c, float s, float cl, float sl) {
+    const float rx = fmaf(a.x, c, fmaf(-a.y, s, fmaf(-a.y, sl, a.x * cl)));
+    const float ry = fmaf(a.x, s, fmaf(a.y, c, fmaf(a.y, cl, a.x * sl)));
+    return make_float2(rx, ry);
+}
+// a * W_R^M (conjugated for INV) with compile-time M, R
+template <bool INV, int M, int R, class C> __device__ __forceinline__ C wmul(C a) {
+    if constexpr (sizeof(decltype(C::x)) == 8) {
+        return cmul(a, wconst<C, INV>(M, R));
+    } else {
+        constexpr double c = cos2pi(M, R), s = INV ? sin2pi(M, R) : -sin2pi(M, R);
+        constexpr float ch = (float)c, sh = (float)s;
+        constexpr float cl = (float)(c - (double)ch), sl = (float)(s - (double)sh);
+        if constexpr (cl == 0.f && sl == 0.f) return cmul(a, make_float2(ch, sh));
+        else return cmul_comp(a, ch, sh, cl, sl);
+    }
+}
+// a * table twiddle m (forward sign stored; conjugated for INV).  FP32 tables
+// carry their lo parts in a second array `lo` of the same length.
+template <bool INV> __device__ __forceinline__ double2 twmul(double2 a, const double2* hi, const double2*, int m) {
+    return cmul(a, tw_get_pre<INV>(hi[m]));
+}
+template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, const float2* hi, const float2* lo, int m) {
+    const float2 h = hi[m], l = lo[m];
+    return INV ? cmul_comp(a, h.x, -h.y, l.x, -l.y) : cmul_comp(a, h.x, h.y, l.x, l.y);
+}
+// x * k for a real constant k: FP64 plain; FP32 with k = hi + lo folded
+template <class T> struct KC;
+template <> struct KC<double> {
+    double v;
+    __device__ __forceinline__ double mul(double x) const { return x * v; }
+};
+template <> struct KC<float> {
+    float hi, lo;
+    __device__ __forceinline__ float mul(float x) const { return fmaf(x, hi, x * lo); }
+};
+
+// compile-time loop: f(std::integral_constant<int, i>) for i in [0, N)
+template <class F, int... Is>
+__device__ __forceinline__ void sfor_impl(F&& f, std::integer_sequence<int, Is...>) {
+    (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F> __device__ __forceinline__ void sfor(F&& f) {
+    sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
 // ------------------------------------------------------------ codelets
 // In-register DFT of size R, natural order in and out:
 // A[k] = sum_j a[j] * W_R^{jk}, W_R = exp(-2 pi i / R) (forward) or its conjugate.
@@ -90,14 +148,22 @@ template <bool INV, class C> struct DFT<2, INV, C> {
 template <bool INV, class C> struct DFT<3, INV, C> {
     static __device__ __forceinline__ void run(C* a) {
         using T = decltype(C::x);
-        const T h = (T)0.86602540378443864676;
         C s = cadd(a[1], a[2]);
         C d = csub(a[1], a[2]);
         C m = cmk<C>(a[0].x - (T)0.5 * s.x, a[0].y - (T)0.5 * s.y);
         C r = cmul_mi<INV>(d);  // -i d (fwd) / +i d (inv)
         a[0] = cadd(a[0], s);
-        a[1] = cmk<C>(m.x + h * r.x, m.y + h * r.y);
-        a[2] = cmk<C>(m.x - h * r.x, m.y - h * r.y);
+        C hr;
+        if constexpr (sizeof(T) == 8) {
+            const T h = (T)0.86602540378443864676;
+            hr = cmk<C>(h * r.x, h * r.y);
+        } else {  // sqrt(3)/2 = hi + lo, folded before the rounding
+            constexpr double hd = 0.86602540378443864676;
+            constexpr float hh = (float)hd, hl = (float)(hd - (double)hh);
+            hr = cmk<C>(fmaf(r.x, hh, r.x * hl), fmaf(r.y, hh, r.y * hl));
+        }
+        a[1] = cmk<C>(m.x + hr.x, m.y + hr.y);
+        a[2] = cmk<C>(m.x - hr.x, m.y - hr.y);
     }
 };
 template <bool INV, class C> struct DFT<4, INV, C> {
@@ -119,16 +185,18 @@ template <int R, bool INV, class C> struct DFT {
     static __device__ __forceinline__ void run(C* a) {
         constexpr int P = Split<R>::P, Q = Split<R>::Q;  // input j = j2 + Q*j1, output k = k1 + P*k2
         C y[R];
-#pragma unroll
-        for (int j2 = 0; j2 < Q; ++j2) {
+        sfor<Q>([&](auto J2) {
+            constexpr int j2 = decltype(J2)::value;
             C t[P];
 #pragma unroll
             for (int j1 = 0; j1 < P; ++j1) t[j1] = a[j2 + Q * j1];
             DFT<P, INV, C>::run(t);
-#pragma unroll
-            for (int k1 = 0; k1 < P; ++k1)
-                y[j2 + Q * k1] = (j2 * k1 == 0) ? t[k1] : cmul(t[k1], wconst<C, INV>((j2 * k1) % R, R));
-        }
+            sfor<P>([&](auto K1) {
+                constexpr int k1 = decltype(K1)::value;
+                if constexpr (j2 * k1 == 0) y[j2 + Q * k1] = t[k1];
+                else y[j2 + Q * k1] = wmul<INV, (j2 * k1) % R, R>(t[k1]);
+            });
+        });
 #pragma unroll
         for (int k1 = 0; k1 < P; ++k1) {
             C t[Q];
@@ -166,11 +234,6 @@ template <int L> __host__ __device__ __forceinline__ int tidx(int p) {
     return (R2 == 1) ? p : (p / R2) + R1 * (p % R2);
 }
 
-// twiddle from a table of W_L^m (forward sign), conjugated for the inverse
-template <bool INV, class C> __device__ __forceinline__ C tw_get(const C* tw, int m) {
-    C w = tw[m];
-    return INV ? cconj(w) : w;
-}
 
 // Line offsets: line l starts at buf + off(l).
 struct LinearLines {
@@ -189,7 +252,7 @@ struct PairRows {
 // NT: natural in -> transposed out.  Lines l in [0, nlines) at buf + off(l),
 // element stride es.  All NTHR threads of the block call it; caller syncs after.
 template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
-__device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* tw) {
+__device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* tw, const C* twlo) {
     constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
     const int tid = threadIdx.x;
@@ -214,7 +277,7 @@ __device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* t
         DFT<R1, INV, C>::run(a);
 #pragma unroll
         for (int k1 = 0; k1 < R1; ++k1) {
-            C v = (k1 == 0) ? a[k1] : cmul(a[k1], tw_get<INV>(tw, (j2 * k1) % L));
+            C v = (k1 == 0) ? a[k1] : twmul<INV>(a[k1], tw, twlo, (j2 * k1) % L);
             p[k1 * R2 * es] = v;
         }
     }
@@ -236,12 +299,12 @@ __device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* t
 // TN: transposed in -> natural out (input element j = j1 + R1 j2 sits at
 // slot j2 + R2 j1, exactly where an NT transform leaves element j).
 template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
-__device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* tw) {
+__device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* tw, const C* twlo) {
     constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
     const int tid = threadIdx.x;
     if constexpr (R2 == 1) {
-        fft_lines_NT<L, INV, NTHR, NLINES, C, OFF>(buf, off, es, tw);
+        fft_lines_NT<L, INV, NTHR, NLINES, C, OFF>(buf, off, es, tw, twlo);
     } else {
     // phase A: for each (line, j1) DFT_R2 over j2 (contiguous block at R2*j1), twiddle W_L^{j1 k2}
     for (int it = tid; it < nlines * R1; it += NTHR) {
@@ -253,7 +316,7 @@ __device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* t
         DFT<R2, INV, C>::run(a);
 #pragma unroll
         for (int k2 = 0; k2 < R2; ++k2) {
-            C v = (k2 == 0) ? a[k2] : cmul(a[k2], tw_get<INV>(tw, (j1 * k2) % L));
+            C v = (k2 == 0) ? a[k2] : twmul<INV>(a[k2], tw, twlo, (j1 * k2) % L);
             p[k2 * es] = v;
         }
     }

@@ -15,6 +15,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "cb_fft.cuh"
+
 namespace cb {
 
 enum Method { M_EULER = 0, M_ETD2 = 1, M_ETD4 = 2 };
@@ -75,6 +77,7 @@ struct Params {
     int etd4_ref;       // 1: reference combine (N_a in the first slot, belastic.cpp:550)
     int kmax;           // largest folded |k|^2 index
     int grow_every;     // grow dt every this many accepted steps
+    int split;          // 1: split plane passes for every xy mode
     double eps, eta, ga, M1, M2;
     double cx;          // (2 pi / L)^2
     double L3;          // box volume
@@ -86,21 +89,31 @@ struct Params {
     // FP32 rate, so kernels read these instead of dividing per thread
     double d_ieps, d_ieps2, d_ieps3, d_bnl;  // 1/eps, 1/eps^2, 1/eps^3, beta * cx
     float f_eps, f_ieps, f_ieps2, f_ieps3, f_bnl, f_cx, f_invN, f_eta;
+    // the same constants split hi + lo for the FP32 form's compensated
+    // products (KC<float>): eps, 1/eps, eta/eps^2, eta D/eps^3, beta cx, 1/N, cx
+    float fk[7][2];
 };
+enum { FK_EPS = 0, FK_IEPS, FK_K2, FK_K3, FK_BNL, FK_INVN, FK_CX };
 
 // the precomputed constants in the kernel's precision
 template <class T> struct PC;
 template <> struct PC<float> {
     float eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    KC<float> k_eps, k_ieps, k_K2, k_K3, k_bnl, k_invN, k_cx;
     __device__ __forceinline__ explicit PC(const Params& p)
         : eps(p.f_eps), ieps(p.f_ieps), ieps2(p.f_ieps2), ieps3(p.f_ieps3), bnl(p.f_bnl), cx(p.f_cx),
-          invN(p.f_invN), eta(p.f_eta) {}
+          invN(p.f_invN), eta(p.f_eta), k_eps{p.fk[FK_EPS][0], p.fk[FK_EPS][1]},
+          k_ieps{p.fk[FK_IEPS][0], p.fk[FK_IEPS][1]}, k_K2{p.fk[FK_K2][0], p.fk[FK_K2][1]},
+          k_K3{p.fk[FK_K3][0], p.fk[FK_K3][1]}, k_bnl{p.fk[FK_BNL][0], p.fk[FK_BNL][1]},
+          k_invN{p.fk[FK_INVN][0], p.fk[FK_INVN][1]}, k_cx{p.fk[FK_CX][0], p.fk[FK_CX][1]} {}
 };
 template <> struct PC<double> {
     double eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    KC<double> k_eps, k_ieps, k_K2, k_K3, k_bnl, k_invN, k_cx;
     __device__ __forceinline__ explicit PC(const Params& p)
         : eps(p.eps), ieps(p.d_ieps), ieps2(p.d_ieps2), ieps3(p.d_ieps3), bnl(p.d_bnl), cx(p.cx), invN(p.invN),
-          eta(p.eta) {}
+          eta(p.eta), k_eps{p.eps}, k_ieps{p.d_ieps}, k_K2{p.eta * p.d_ieps2}, k_K3{p.eta * 1.5 * p.d_ieps3},
+          k_bnl{p.d_bnl}, k_invN{p.invN}, k_cx{p.cx} {}
 };
 
 // exit reasons kept in Ctrl::status (mirrors the public CB_* codes)
@@ -116,6 +129,7 @@ template <class T> struct InstT {
     void* P[3][2];  // partial sets: [0],[1] state/candidate (swap via ctrl->part_state), [2] work
     void* A;
     void* B;
+    void* Y[2];       // split plane path: y-transformed fields (nullptr when unused)
     T* coef;          // kNTab tables of (kmax + 1) * 8 entries
     Ctrl* ctrl;
     double* part_xy;  // [nz][4] per-plane partial sums

@@ -29,6 +29,18 @@ enum ZMode {
     Z_INV_PLAIN,    // spectrum (x multiplier) -> partial P0
 };
 
+// y-column pass of the split plane path (split_kernels.cuh)
+enum YMode { Y_INV2 = 0, Y_INV1, Y_FWD2, Y_FWD1 };
+
+struct YArgs {
+    int mode;
+    int role;           // stepping: partial set read (inverse)
+    int stepping;       // 1: instance buffers (P / Y / A, B) and the done / stale checks
+    int skip_if_stale;
+    const void* cin;    // plain inverse: partial C[nz][ny][nc]
+    void* cout;         // plain forward: partial C[nz][ny][nc]
+};
+
 enum SpecMul { SM_NONE = 0, SM_LAP = 1, SM_DX = 2, SM_DY = 3, SM_DZ = 4 };
 
 // state_io bits for the plain z modes: the spectrum read (1) or written (2) is

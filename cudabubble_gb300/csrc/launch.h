@@ -9,15 +9,22 @@
 namespace cb {
 
 template <class T> struct Launch {
-    static bool xy_supported(int nx);
+    static bool xy_supported(int nx);        // stepping (single-CTA planes or the split path)
     static bool z_supported(int nz);
-    static bool xy_plain_supported(int nx);
+    static bool xy_plain_supported(int nx);  // plain transforms
+    static bool xy_single(int nx, int nf);   // one CTA per plane holds nf fields
+    static bool xy_split_supported(int nx);
+    static int xy_rows_per_cta(int nx);      // split path: rows of the x pass per CTA
     static int z_tile();
-    static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s);
+    // split: 1 forces the split plane path, 0 uses it only where a plane does not fit one CTA
+    static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
+                          int split = 0);
     static cudaError_t z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s);
     static cudaError_t decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s);
     static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw = 1);
     static cudaError_t to_double(const void* in, double* out, size_t n, cudaStream_t s);
+    // the full ETD N-hat of instance 0 (its Nu buffer, plus the FP32 form's linear part on `spec`)
+    static cudaError_t nhat_full(const InstT<T>* d, const void* spec, double* out, size_t n, cudaStream_t s);
     static cudaError_t state_to_double(const void* in, double* out, size_t n, cudaStream_t s);
     // complex double spectrum <-> stepped state of precision T (to_state = 1: double -> state)
     static cudaError_t f64_to_state(const void* in, void* out, size_t n, int to_state, cudaStream_t s);

@@ -1,8 +1,11 @@
 // Size dispatch for the kernel templates (included by kernels_f32.cu and
 // kernels_f64.cu with CB_REAL set to float or double).
 #pragma once
+#include <string.h>
+
 #include "launch.h"
 #include "misc_kernels.cuh"
+#include "split_kernels.cuh"
 #include "xy_kernel.cuh"
 #include "z_kernel.cuh"
 
@@ -44,6 +47,80 @@ static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& 
 
 template <class T> constexpr int ztile() { return sizeof(T) == 4 ? 16 : 8; }
 
+// ---- split plane path
+template <int NX> constexpr int split_rpc() { return NX >= 96 ? 16 : 8; }
+constexpr int kSplitThreads = 256;
+
+template <class T, int NY>
+static cudaError_t ycol_go(const InstT<T>* d, int ninst, int nzmax, const YArgs& a, cudaStream_t s) {
+    constexpr int TX = ztile<T>(), NT = kSplitThreads;
+    constexpr size_t sm = ycol_smem_bytes<T, NY, TX>();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(ycol_kernel<T, NY, TX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int ntx = (NY / 2 + 1 + TX - 1) / TX;  // square planes: nc = NY/2 + 1
+    ycol_kernel<T, NY, TX, NT><<<dim3(nzmax * ntx, ninst), NT, sm, s>>>(d, a);
+    return cudaGetLastError();
+}
+
+template <class T, int NX>
+static cudaError_t xrow_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    constexpr int RPC = split_rpc<NX>(), NT = kSplitThreads;
+    constexpr size_t sm = xrow_smem_bytes<T, NX, RPC>();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(xrow_kernel<T, NX, RPC, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    xrow_kernel<T, NX, RPC, NT><<<dim3(nzmax * NX / RPC, ninst), NT, sm, s>>>(d, a);
+    return cudaGetLastError();
+}
+
+// one xy mode as y pass(es) around the x-row pass
+template <class T, int NX>
+static cudaError_t xy_split_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    YArgs y;
+    memset(&y, 0, sizeof y);
+    y.role = a.role;
+    y.stepping = a.mode <= XY_NONLIN;
+    y.skip_if_stale = a.skip_if_stale;
+    cudaError_t r = cudaSuccess;
+    switch (a.mode) {
+        case XY_NONLIN:
+        case XY_REDUCE_FULL:
+            y.mode = Y_INV2;
+            break;
+        case XY_REDUCE_S:
+            y.mode = Y_INV1;
+            break;
+        case XY_INV_PLAIN:
+            y.mode = Y_INV1;
+            y.cin = a.cin;
+            break;
+        default:  // XY_FWD_PLAIN: rows first
+            y.mode = -1;
+            break;
+    }
+    if (y.mode >= 0) {
+        r = ycol_go<T, NX>(d, ninst, nzmax, y, s);
+        if (r != cudaSuccess) return r;
+    }
+    r = xrow_go<T, NX>(d, ninst, nzmax, a, s);
+    if (r != cudaSuccess) return r;
+    if (a.mode == XY_NONLIN || a.mode == XY_FWD_PLAIN) {
+        y.mode = a.mode == XY_NONLIN ? Y_FWD2 : Y_FWD1;
+        y.cout = a.cout;
+        r = ycol_go<T, NX>(d, ninst, nzmax, y, s);
+    }
+    return r;
+}
+
 template <class T, int NZ>
 static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
     constexpr int TX = ztile<T>();
@@ -62,22 +139,25 @@ static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a
 #define CB_XY_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128)
 #define CB_Z_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
 
-template <class T> bool Launch<T>::xy_supported(int nx) {
+template <class T> bool Launch<T>::xy_single(int nx, int nf) {
     switch (nx) {
-#define CASE(n) case n: return XYCfg<T, n>::ok;
+#define CASE(n) case n: return nf == 2 ? XYCfg<T, n>::ok : XYCfg<T, n>::ok1;
         CB_XY_SIZES(CASE)
 #undef CASE
         default: return false;
     }
 }
-template <class T> bool Launch<T>::xy_plain_supported(int nx) {
+template <class T> bool Launch<T>::xy_split_supported(int nx) {
     switch (nx) {
-#define CASE(n) case n: return XYCfg<T, n>::ok1;
-        CB_XY_SIZES(CASE)
+#define CASE(n) case n: return true;
+        CB_Z_SIZES(CASE)
 #undef CASE
         default: return false;
     }
 }
+template <class T> int Launch<T>::xy_rows_per_cta(int nx) { return nx >= 96 ? 16 : 8; }
+template <class T> bool Launch<T>::xy_supported(int nx) { return xy_single(nx, 2) || xy_split_supported(nx); }
+template <class T> bool Launch<T>::xy_plain_supported(int nx) { return xy_single(nx, 1) || xy_split_supported(nx); }
 template <class T> bool Launch<T>::z_supported(int nz) {
     switch (nz) {
 #define CASE(n) case n: return true;
@@ -89,10 +169,20 @@ template <class T> bool Launch<T>::z_supported(int nz) {
 template <class T> int Launch<T>::z_tile() { return ztile<T>(); }
 
 template <class T>
-cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
-    switch (nx) {
+cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
+                          int split) {
+    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
+    if (!split && xy_single(nx, nf)) {
+        switch (nx) {
 #define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s);
-        CB_XY_SIZES(CASE)
+            CB_XY_SIZES(CASE)
+#undef CASE
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (nx) {
+#define CASE(n) case n: return xy_split_go<T, n>(d, ninst, nzmax, a, s);
+        CB_Z_SIZES(CASE)
 #undef CASE
         default: return cudaErrorInvalidValue;
     }
@@ -120,6 +210,13 @@ template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int
 template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out, size_t n, cudaStream_t s) {
     const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     cplx_to_double_kernel<T><<<blocks, 256, 0, s>>>(reinterpret_cast<const cplx<T>*>(in), reinterpret_cast<double2*>(out), n);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t Launch<T>::nhat_full(const InstT<T>* d, const void* spec, double* out, size_t n, cudaStream_t s) {
+    const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    nhat_full_kernel<T><<<blocks, 256, 0, s>>>(d, spec, reinterpret_cast<double2*>(out));
     return cudaGetLastError();
 }
 

@@ -61,13 +61,27 @@ __global__ void prologue_kernel(const InstT<T>* __restrict__ insts, int n, int r
     c->fill_slot = j;
 }
 
+// Linear part of the ETD nonlinearity, c_lin(k) = eta kappa (D / eps^3 + cx |k|^2 / eps):
+// N-hat = N'-hat + c_lin u-hat, with N' formed from G' = G - eta D kappa u / eps^3 and
+// H' = H + kappa u = (u^2 - 1) u, both small where u = +-1.  The FP32 form transforms
+// only G', H' and applies c_lin u-hat to the exact (double-float) spectrum through its
+// table: the bulk terms of G (~eta D kappa / eps^3, thousands) otherwise carry FP32
+// transform and rounding errors into the k ~ 0 modes, which the energy amplifies.
+__device__ inline double lin_coef(const Params& p, int k2) {
+    const double kappa = 2.0, D = 1.5;
+    return p.eta * kappa * (D * p.d_ieps3 + p.cx * (double)k2 * p.d_ieps);
+}
+
 // Fills the table slot the prologue selected (grid: blocks x instances).
 // L(k) follows Calc.cu:579-606 with c = -cx |k|^2 (kappa = 2, D = 1.5).
 // accurate == 0 evaluates the reference's own closed forms (Calc.cu:446-569);
 // accurate == 1 uses phi-functions, free of the small-|hL| cancellation.
-// The FP32 form stores em = exp(hL) - 1 in place of the exponential factors
-// (slots 0 and 2): its state update is base + (em base + increment) in
-// double-float arithmetic (z_kernel.cuh, State<float>).
+// The FP32 form stores, for the split N-hat = N'-hat + c_lin u-hat (lin_coef),
+//   ETD-RK2: em' = c1 L' (L' = L + c_lin), c1, c2, c2 c_lin
+//   ETD-RK4: em'_h = c_h L', c_h, em'_4 = exp(hL) - 1 + c_lin (f1 + 2 f2 + f3),
+//            f1, f2, f3, c_h c_lin, c_lin
+// and its state update is base (+) (em' base + increment) in double-float
+// arithmetic (z_kernel.cuh, State<float>).
 template <class T>
 __global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurate) {
     const InstT<T>& I = insts[blockIdx.y];
@@ -97,7 +111,14 @@ __global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurat
                 c2 = (dt * L == 0.0) ? dt / 2 : (e1 - 1.0 - dt * L) / (dt * L * L);
                 x0 = (sizeof(T) == 4) ? e1 - 1.0 : e1;
             }
-            out[0] = (T)x0; out[1] = (T)c1; out[2] = (T)c2;
+            if constexpr (sizeof(T) == 4) {  // the linear-split form (see lin_coef)
+                const double cl = lin_coef(p, idx);
+                out[0] = (T)(c1 * (L + cl));  // em' = (exp(hL) - 1) L' / L
+                out[3] = (T)(c2 * cl);
+            } else {
+                out[0] = (T)x0;
+            }
+            out[1] = (T)c1; out[2] = (T)c2;
         } else {
             double x0, x2, ch, f1, f2, f3;
             if (accurate) {
@@ -120,7 +141,16 @@ __global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurat
                 x0 = (sizeof(T) == 4) ? eh - 1.0 : eh;
                 x2 = (sizeof(T) == 4) ? e2 - 1.0 : e2;
             }
-            out[0] = (T)x0; out[1] = (T)ch; out[2] = (T)x2; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
+            if constexpr (sizeof(T) == 4) {
+                const double cl = lin_coef(p, idx);
+                out[0] = (T)(ch * (L + cl));                        // em'_h
+                out[2] = (T)(x2 + cl * (f1 + 2.0 * f2 + f3));       // em'_4
+                out[6] = (T)(ch * cl);
+                out[7] = (T)cl;
+            } else {
+                out[0] = (T)x0; out[2] = (T)x2;
+            }
+            out[1] = (T)ch; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
         }
     }
     __syncthreads();
@@ -261,6 +291,29 @@ __global__ void f64_state_kernel(const void* __restrict__ in, void* __restrict__
         } else {
             reinterpret_cast<double2*>(out)[i] = reinterpret_cast<const double2*>(in)[i];
         }
+    }
+}
+
+// full N-hat = N'-hat + c_lin u-hat of the FP32 form's split (lin_coef), in FP64,
+// for the field getter; the FP64 form keeps the full N-hat in Nu
+template <class T>
+__global__ void nhat_full_kernel(const InstT<T>* __restrict__ insts, const void* __restrict__ spec,
+                                 double2* __restrict__ out) {
+    const InstT<T>& I = insts[0];
+    const Params& p = I.p;
+    const size_t n = (size_t)p.nz * p.ny * p.nc;
+    const cplx<T>* nu = reinterpret_cast<const cplx<T>*>(I.Nu);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double2 v = make_double2((double)nu[i].x, (double)nu[i].y);
+        if (sizeof(T) == 4) {
+            const int kx = (int)(i % p.nc), ky = (int)((i / p.nc) % p.ny), kz = (int)(i / ((size_t)p.nc * p.ny));
+            const int kyf = min(ky, p.ny - ky), kzf = min(kz, p.nz - kz);
+            const double cl = lin_coef(p, kx * kx + kyf * kyf + kzf * kzf);
+            const float4 q = reinterpret_cast<const float4*>(spec)[i];
+            v.x += cl * ((double)q.x + (double)q.z);
+            v.y += cl * ((double)q.y + (double)q.w);
+        }
+        out[i] = v;
     }
 }
 

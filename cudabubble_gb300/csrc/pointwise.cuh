@@ -1,0 +1,87 @@
+// Pointwise stages shared by the single-CTA xy pass (xy_kernel.cuh) and the
+// row pass of the split plane path (split_kernels.cuh): the nonlinear
+// partials G, H and the energy / area sums, on real values held as the two
+// halves of complex slots.
+#pragma once
+#include "cb_fft.cuh"
+#include "cb_inst.h"
+
+namespace cb {
+
+template <class T> struct Acc;
+template <> struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double part() const { return s; }
+};
+// FP32 values summed as a double-float pair (error-free TwoSum per add)
+template <> struct Acc<float> {
+    FF v{0.f, 0.f};
+    __device__ __forceinline__ void add(float x) { v = ff_add(v, FF{x, 0.f}); }
+    __device__ __forceinline__ FF part() const { return v; }
+};
+
+// lambda_1 = M1 (V - alpha), lambda_2 = M2 (S - beta) (belastic.cpp:478-479) as
+// the constant and f coefficients of G, formed in FP64 by one thread.
+template <class T> __device__ __forceinline__ void nonlin_lambdas(const Params& p, const Ctrl* ctrl, int role, T* lam) {
+    const bool euler = p.method == M_EULER;
+    const Scal& sc = ctrl->sc[role];
+    const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
+    lam[0] = euler ? (T)(0.5 * lam1) : (T)(-0.5 * lam1);
+    lam[1] = euler ? (T)lam2 : (T)(-lam2 * 1.0606601717798212866);  // 3 / (2 sqrt 2)
+}
+
+// G, H of one real point from u and lap u:
+// ETD  (Calc.cu:428-437 with nld from :265-284):
+//   G = -lam1/2 - c3 lam2 f - eta (D t / eps^3 + (3u^2 - D - 1) f / eps^2),  H = t
+// Euler (Calc.cu:410-419 with g0 from :171-180):
+//   G = lam1/2 + lam2 f + eta (3u^2 - 1) f / eps^2,                         H = f
+// with f = -eps lap + (u^2 - 1) u / eps and t = u (u^2 - 1 - kappa), kappa = 2,
+// D = 1.5 (phasefield.cpp:259-260).  The FP32 form folds every constant hi + lo.
+template <class T>
+__device__ __forceinline__ void nonlin_point(const PC<T>& k, bool euler, T g_c, T g_f, T u, T lap, T& g, T& h) {
+    const T kappa = (T)2.0, D = (T)1.5;
+    const T u2 = u * u;
+    if constexpr (sizeof(T) == 8) {
+        const T f = -lap * k.eps + (u2 - (T)1) * u * k.ieps;
+        if (euler) {
+            g = g_c + g_f * f + k.eta * ((T)3 * u2 - (T)1) * f * k.ieps2;
+            h = f;
+        } else {
+            const T t = u * (u2 - (T)1 - kappa);
+            g = g_c + g_f * f - k.eta * (D * t * k.ieps3 + ((T)3 * u2 - D - (T)1) * k.ieps2 * f);
+            h = t;
+        }
+    } else {
+        const T w = (u2 - (T)1) * u;
+        const T f = k.k_ieps.mul(w) - k.k_eps.mul(lap);
+        if (euler) {
+            g = g_c + g_f * f + k.k_K2.mul(((T)3 * u2 - (T)1) * f);
+            h = f;
+        } else {
+            // ETD in the linear-split form: G' = G - eta D kappa u / eps^3 and
+            // H' = t + kappa u = w; the kappa u parts are applied to the exact
+            // spectrum in the z pass (misc_kernels.cuh, lin_coef)
+            g = g_c + g_f * f - (k.k_K3.mul(w) + k.k_K2.mul(((T)3 * u2 - D - (T)1) * f));
+            h = w;
+        }
+        (void)kappa;
+    }
+}
+
+// sums of one real point: u, (u^2 - 1)^2 and (full) f^2 (phasefield.cpp:283-325)
+template <class T>
+__device__ __forceinline__ void reduce_point(const PC<T>& k, bool full, T u, T lap, Acc<T>& au, Acc<T>& as,
+                                             Acc<T>& af) {
+    const T u2m = u * u - (T)1;
+    au.add(u);
+    as.add(u2m * u2m);
+    if (full) {
+        T f;
+        if constexpr (sizeof(T) == 8) f = -lap * k.eps + u2m * u * k.ieps;
+        else f = k.k_ieps.mul(u2m * u) - k.k_eps.mul(lap);
+        af.add(f * f);
+    }
+}
+
+}  // namespace cb

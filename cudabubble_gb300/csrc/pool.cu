@@ -62,7 +62,7 @@ __global__ void ellipsoid_kernel(double* __restrict__ out, int nx, int nz, doubl
 }
 
 template <class T> struct PoolClass {
-    int nx = 0, nz = 0, method = 0, accurate = 0, cap = 0, ntiles = 0;
+    int nx = 0, nz = 0, method = 0, accurate = 0, cap = 0, ntiles = 0, split = 0;
     InstT<T>* table = nullptr;
     SlotSummary* sum = nullptr;
     std::vector<Stepper<T>*> occ;
@@ -99,17 +99,19 @@ template <class T> class Pool {
         return CB_OK;
     }
 
-    int find(int nx, int nz, int method, int accurate) const {
+    int find(int nx, int nz, int method, int accurate, int split) const {
         for (size_t i = 0; i < cls.size(); ++i)
-            if (cls[i].nx == nx && cls[i].nz == nz && cls[i].method == method && cls[i].accurate == accurate)
+            if (cls[i].nx == nx && cls[i].nz == nz && cls[i].method == method && cls[i].accurate == accurate &&
+                cls[i].split == split)
                 return (int)i;
         return -1;
     }
 
-    int add_class(int nx, int nz, int method, int accurate, int ntiles, int cap) {
+    int add_class(int nx, int nz, int method, int accurate, int split, int ntiles, int cap) {
         if (g) return fail(CB_EINVAL, "pool graph already built");
         PoolClass<T> c;
         c.nx = nx; c.nz = nz; c.method = method; c.accurate = accurate; c.cap = cap; c.ntiles = ntiles;
+        c.split = split;
         c.occ.assign(cap, nullptr);
         CB_CK(cudaMalloc(&c.table, sizeof(InstT<T>) * cap));
         CB_CK(cudaMalloc(&c.sum, sizeof(SlotSummary) * cap));
@@ -125,7 +127,7 @@ template <class T> class Pool {
     // put an instance into a free slot of its class
     int place(Stepper<T>* sp, int* ci, int* si) {
         const Params& p = sp->params();
-        const int c = find(p.nx, p.nz, p.method, sp->accurate());
+        const int c = find(p.nx, p.nz, p.method, sp->accurate(), p.split);
         if (c < 0) return fail(CB_EINVAL, "no size class for %dx%dx%d", p.nx, p.ny, p.nz);
         for (int k = 0; k < cls[c].cap; ++k) {
             if (!cls[c].occ[k]) {
@@ -164,7 +166,7 @@ template <class T> class Pool {
             if (r == cudaSuccess) r = cudaEventRecord(c.fork, st);
             if (r == cudaSuccess) r = cudaStreamWaitEvent(c.s, c.fork, 0);
             if (r == cudaSuccess)
-                r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false, c.s);
+                r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false, c.split, c.s);
             if (r == cudaSuccess) r = cudaEventRecord(c.join, c.s);
             if (r == cudaSuccess) r = cudaStreamWaitEvent(st, c.join, 0);
         }
@@ -247,13 +249,13 @@ template <class T> class Batch final : public BatchBase {
         }
         for (auto& it : items) {
             const Params& p = it->params();
-            if (pool->find(p.nx, p.nz, p.method, it->accurate()) >= 0) continue;
+            if (pool->find(p.nx, p.nz, p.method, it->accurate(), p.split) >= 0) continue;
             int cap = 0;
             for (auto& jt : items) {
                 const Params& q = jt->params();
                 if (q.nx == p.nx && q.nz == p.nz && q.method == p.method && jt->accurate() == it->accurate()) ++cap;
             }
-            rc = pool->add_class(p.nx, p.nz, p.method, it->accurate(), it->tiles(), cap);
+            rc = pool->add_class(p.nx, p.nz, p.method, it->accurate(), p.split, it->tiles(), cap);
             if (rc) return rc;
         }
         where.resize(n);
@@ -393,12 +395,12 @@ static int serve_impl(const cb_request* reqs, int n, long long budget, int max_s
         if (rc) return rc;
         if (!Launch<T>::xy_supported(e.p.nx) || !Launch<T>::z_supported(e.p.nz))
             return fail(CB_EUNSUPPORTED, "request %d: grid %d^2x%d not built", i, e.p.nx, e.p.nz);
-        if (pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate) >= 0) continue;
+        if (pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split) >= 0) continue;
         const long long bytes = (long long)instance_arena_bytes<T>(e.p);
         int cap = (int)std::min<long long>(max_slots, budget / std::max<long long>(bytes, 1));
         cap = std::max(cap, 1);
         const int tx = Launch<T>::z_tile();
-        rc = pool.add_class(e.p.nx, e.p.nz, e.p.method, e.accurate, (e.p.ny * e.p.nc + tx - 1) / tx, cap);
+        rc = pool.add_class(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split, (e.p.ny * e.p.nc + tx - 1) / tx, cap);
         if (rc) return rc;
     }
     rc = pool.build_graph();
@@ -431,7 +433,7 @@ static int serve_impl(const cb_request* reqs, int n, long long budget, int max_s
             Eff e;
             make_params(reqs[i].params, e);
             const long long bytes = (long long)instance_arena_bytes<T>(e.p);
-            const int c = pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate);
+            const int c = pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split);
             if (used + bytes > budget || !pool.has_free(c)) break;
             Active<T> a;
             a.st.reset(new Stepper<T>());

@@ -71,15 +71,19 @@ template <class T> inline void* twiddle_table(int n, int xkind, cudaError_t* err
     auto it = g_tw.find(key);
     if (it != g_tw.end()) return it->second;
     std::vector<T> v;
+    std::vector<long double> ex;  // the exact values, for the FP32 lo parts
     auto push = [&](int len) {
         for (int m = 0; m < len; ++m) {
             const long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)len;
-            v.push_back((T)cosl(a));
-            v.push_back((T)(-sinl(a)));
+            ex.push_back(cosl(a));
+            ex.push_back(-sinl(a));
         }
     };
     if (xkind) push(n / 2);  // half-length transform table, then the full one
     push(n);
+    for (long double x : ex) v.push_back((T)x);
+    if (sizeof(T) == 4)  // FP32: lo = fl(exact - hi), in the same order after the hi parts
+        for (size_t i = 0; i < ex.size(); ++i) v.push_back((T)(ex[i] - (long double)v[i]));
     void* d = nullptr;
     *err = cudaMalloc(&d, v.size() * sizeof(T));
     if (*err != cudaSuccess) return nullptr;
@@ -140,6 +144,7 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.kmax = (p.nx / 2) * (p.nx / 2) + (p.ny / 2) * (p.ny / 2) + (p.nz / 2) * (p.nz / 2);
     const bool euler = u.method == CB_EULER;
     p.grow_every = u.grow_every > 0 ? u.grow_every : 4;
+    p.split = u.xy_split ? 1 : 0;
     p.grow_factor = u.grow_factor > 0 ? u.grow_factor : (euler ? 1.4 : 2.0);
     p.dt_cap = u.dt_cap > 0 ? u.dt_cap : (euler ? 1e300 : 1e-3);
     p.cap_probe = u.cap_probe > 0 ? u.cap_probe : (euler ? 0.0 : 1.4);
@@ -161,6 +166,14 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.f_cx = (float)p.cx;
     p.f_invN = (float)p.invN;
     p.f_eta = (float)p.eta;
+    {
+        const double k[7] = {p.eps, p.d_ieps, p.eta * p.d_ieps2, p.eta * 1.5 * p.d_ieps3, p.d_bnl, p.invN, p.cx};
+        for (int i = 0; i < 7; ++i) {
+            const float hi = (float)k[i];
+            p.fk[i][0] = hi;
+            p.fk[i][1] = (float)(k[i] - (double)hi);
+        }
+    }
     const double ts = u.time_step > 0 ? u.time_step : 1e-6;  // fluidbase.cpp:112
     e.dt0 = p.adaptive ? ts : std::min(u.fixed_time_step, ts);  // belastic.cpp:599-602
     e.precision = u.precision;
@@ -193,7 +206,7 @@ enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, 
 // event pair brackets every launch and is appended as (kind, start, end).
 template <class T>
 inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, int ninst, int ntiles, int accurate,
-                                 bool raw, cudaStream_t s,
+                                 bool raw, int split, cudaStream_t s,
                                  std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
     cudaError_t r = cudaSuccess;
     auto timed = [&](int kind, auto&& fn) {
@@ -215,7 +228,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             a.mode = m;
             a.role = role;
             a.skip_if_stale = skip;
-            return Launch<T>::xy(nx, d, ninst, nz, a, s);
+            return Launch<T>::xy(nx, d, ninst, nz, a, s, split);
         });
     };
     auto Z = [&](int m, int role) {
@@ -265,21 +278,35 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
 // Arena of one instance.  Stepped-state spectra (phi-hat x2, a-hat) hold 16
 // bytes per mode in both forms (FP64 complex, or FP32 double-float pairs);
 // every other field is one complex T per mode.
+// the split plane path is used for some xy mode of this precision and grid
+template <class T> inline bool uses_split(const Params& p) {
+    return p.split || !Launch<T>::xy_single(p.nx, 2) || !Launch<T>::xy_single(p.nx, 1);
+}
+// per-plane or per-row-block partial sums of the xy reductions
+template <class T> inline size_t xy_part_slots(const Params& p) {
+    size_t n = (size_t)p.nz;
+    if (uses_split<T>(p)) n = std::max(n, (size_t)p.nz * p.ny / Launch<T>::xy_rows_per_cta(p.nx));
+    return n;
+}
+
 template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* layout = nullptr) {
     const size_t ns = (size_t)p.nz * p.ny * p.nc;
     const int ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t fs = al(ns * 16), fp = al(ns * sizeof(T) * 2);
-    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0);  // Nu, P x6, A, B (+ Na, Nb)
+    // Nu, P x6, A, B (+ Na, Nb), then the split path's Y0, Y1
+    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0);
+    // FP32 form: the FP64 plain transforms of set/get phi need their own Y0, Y1
+    const int naux = (sizeof(T) == 4 && uses_split<double>(p)) ? 2 : 0;
     size_t off = 0;
     if (layout) layout[0] = off;
-    off += 3 * fs;
+    off += (3 + naux) * fs;
     if (layout) layout[6] = off;
     off += nplain * fp;
     if (layout) layout[1] = off;
     off += al((size_t)kNTab * (p.kmax + 1) * 8 * sizeof(T));
     if (layout) layout[2] = off;
-    off += al((size_t)p.nz * 4 * sizeof(double));
+    off += al(xy_part_slots<T>(p) * 4 * sizeof(double));
     if (layout) layout[3] = off;
     off += al((size_t)ntiles * 2 * sizeof(double));
     if (layout) layout[4] = off;
@@ -331,6 +358,8 @@ template <class T> class Stepper final : public Handle {
                         &h.A, &h.B, &h.Na, &h.Nb};
         const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0);
         for (int i = 0; i < nplain; ++i) *f[i] = base + lay[6] + i * fp;
+        if (uses_split<T>(p))
+            for (int i = 0; i < 2; ++i) h.Y[i] = base + lay[6] + (nplain + i) * fp;
         h.coef = reinterpret_cast<T*>(base + lay[1]);
         h.part_xy = reinterpret_cast<double*>(base + lay[2]);
         h.part_z = reinterpret_cast<double*>(base + lay[3]);
@@ -354,6 +383,9 @@ template <class T> class Stepper final : public Handle {
             x.ctrl = h.ctrl;
             x.coef = nullptr;
             x.p = p;
+            x.part_xy = h.part_xy;  // plain modes write no sums; kept valid all the same
+            if (uses_split<double>(p))
+                for (int i = 0; i < 2; ++i) x.Y[i] = base + lay[0] + (3 + i) * fs;
             x.twx = twiddle_table<double>(p.nx, 1, &err);
             x.twy = twiddle_table<double>(p.ny, 0, &err);
             x.twz = twiddle_table<double>(p.nz, 0, &err);
@@ -636,7 +668,7 @@ template <class T> class Stepper final : public Handle {
                 CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
                 CB_CK(xypass(XY_NONLIN, R_STATE));
                 CB_CK(zpass(etd ? (p.method == M_ETD2 ? Z_ETD2_S1 : Z_ETD4_S1) : Z_EULER, etd ? R_WORK : R_CAND));
-                if (etd) CB_CK(Launch<T>::to_double(h.Nu, dst, ns, st));
+                if (etd) CB_CK(Launch<T>::nhat_full(d, h.spec[hc.spec_state], dst, ns, st));
                 else CB_CK(inv3d(h.Nu, SM_NONE, dst));
                 break;
             }
@@ -763,7 +795,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = mode;
         a.role = role;
         a.skip_if_stale = skip;
-        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st, p.split);
     }
     cudaError_t zpass(int mode, int role) {
         ZArgs a;
@@ -780,7 +812,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = XY_FWD_PLAIN;
         a.rin = src;
         a.cout = part;
-        cudaError_t r = Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+        cudaError_t r = Launch<T>::xy(p.nx, d, 1, p.nz, a, st, p.split);
         if (r != cudaSuccess) return r;
         ZArgs z;
         memset(&z, 0, sizeof z);
@@ -797,7 +829,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = XY_FWD_PLAIN;
         a.rin = src;
         a.cout = part64;
-        cudaError_t r = Launch<double>::xy(p.nx, aux, 1, p.nz, a, st);
+        cudaError_t r = Launch<double>::xy(p.nx, aux, 1, p.nz, a, st, p.split);
         if (r != cudaSuccess) return r;
         ZArgs z;
         memset(&z, 0, sizeof z);
@@ -819,7 +851,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = XY_INV_PLAIN;
         a.cin = part64;
         a.rout = dst;
-        return Launch<double>::xy(p.nx, aux, 1, p.nz, a, st);
+        return Launch<double>::xy(p.nx, aux, 1, p.nz, a, st, p.split);
     }
     int ntiles64() const { return (p.ny * p.nc + Launch<double>::z_tile() - 1) / Launch<double>::z_tile(); }
     // spectrum (x multiplier) -> real double field, through `part`
@@ -839,7 +871,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = XY_INV_PLAIN;
         a.cin = part;
         a.rout = dst;
-        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st);
+        return Launch<T>::xy(p.nx, d, 1, p.nz, a, st, p.split);
     }
     int ensure_scratch() {
         if (scratch) return CB_OK;
@@ -857,7 +889,7 @@ template <class T> class Stepper final : public Handle {
     }
     // prof != nullptr: record an event pair around every launch (profiling; not captured)
     int enqueue_attempt(bool raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
-        cudaError_t r = enqueue_group<T>(p.method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw, st, prof);
+        cudaError_t r = enqueue_group<T>(p.method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw, p.split, st, prof);
         if (r != cudaSuccess) return fail(CB_ECUDA, "enqueue attempt: %s", cudaGetErrorString(r));
         return CB_OK;
     }

@@ -21,21 +21,9 @@
 #include "cb_fft.cuh"
 #include "cb_inst.h"
 #include "cb_kargs.h"
+#include "pointwise.cuh"
 
 namespace cb {
-
-template <class T> struct Acc;
-template <> struct Acc<double> {
-    double s = 0.0;
-    __device__ __forceinline__ void add(double x) { s += x; }
-    __device__ __forceinline__ double part() const { return s; }
-};
-// FP32 values summed as a double-float pair (error-free TwoSum per add)
-template <> struct Acc<float> {
-    FF v{0.f, 0.f};
-    __device__ __forceinline__ void add(float x) { v = ff_add(v, FF{x, 0.f}); }
-    __device__ __forceinline__ FF part() const { return v; }
-};
 
 __device__ __forceinline__ int part_set(const Ctrl* ctrl, int role) {
     return role == R_WORK ? 2 : (role == R_STATE ? ctrl->part_state : 1 - ctrl->part_state);
@@ -82,13 +70,22 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     C* twM = S + NY * pitch;                // W_M^m
     C* twN = twM + M;                       // W_NX^m
     C* twY = twN + NX;                      // W_NY^m
-    double* red = reinterpret_cast<double*>(twY + NY);
+    // FP32: lo parts of the three tables (same order), FP64: unused aliases
+    constexpr int ntw = sizeof(T) == 4 ? 2 : 1;
+    C* twMl = twY + NY;
+    C* twNl = twMl + M;
+    C* twYl = twNl + NX;
+    double* red = reinterpret_cast<double*>(twM + ntw * (M + NX + NY));
 
     {
         const C* gx = reinterpret_cast<const C*>(I.twx);
         const C* gy = reinterpret_cast<const C*>(I.twy);
         for (int i = tid; i < M + NX; i += NT) twM[i] = gx[i];  // twM and twN are contiguous
         for (int i = tid; i < NY; i += NT) twY[i] = gy[i];
+        if constexpr (ntw == 2) {  // the tables' lo parts follow their hi parts
+            for (int i = tid; i < M + NX; i += NT) twMl[i] = gx[M + NX + i];
+            for (int i = tid; i < NY; i += NT) twYl[i] = gy[NY + i];
+        }
     }
     const T cx = PC<T>(p).cx;
     const size_t plane = (size_t)NY * NC;
@@ -124,23 +121,36 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             }
             if (nf == 2) {  // laplacian partial Q = -cx (kx^2 + ky^2) P0 + P2 (Calc.cu:107-124)
                 const int kyf = min(ky, NY - ky);
-                const T kyy = cx * (T)(kyf * kyf);
                 const C w = P2[ky * NC + c];
-                if (c == 0) {
-                    const C wN = P2[ky * NC + M];
-                    const T kN = cx * (T)(M * M) + kyy;
-                    const C q0 = cmk<C>(w.x - kyy * v.x, w.y - kyy * v.y);
-                    const C qN = cmk<C>(wN.x - kN * vN.x, wN.y - kN * vN.y);
-                    S[ky * pitch + M] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
-                } else {
-                    const T k2 = cx * (T)(c * c) + kyy;
-                    S[ky * pitch + M + c] = cmk<C>(w.x - k2 * v.x, w.y - k2 * v.y);
+                if constexpr (sizeof(T) == 8) {
+                    const T kyy = cx * (T)(kyf * kyf);
+                    if (c == 0) {
+                        const C wN = P2[ky * NC + M];
+                        const T kN = cx * (T)(M * M) + kyy;
+                        const C q0 = cmk<C>(w.x - kyy * v.x, w.y - kyy * v.y);
+                        const C qN = cmk<C>(wN.x - kN * vN.x, wN.y - kN * vN.y);
+                        S[ky * pitch + M] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
+                    } else {
+                        const T k2 = cx * (T)(c * c) + kyy;
+                        S[ky * pitch + M + c] = cmk<C>(w.x - k2 * v.x, w.y - k2 * v.y);
+                    }
+                } else {  // integer |k|^2 exact in FP32, cx folded hi + lo
+                    const KC<T> kcx = PC<T>(p).k_cx;
+                    auto q = [&](C ww, C vv, int kk) {
+                        return cmk<C>(ww.x - kcx.mul((T)kk * vv.x), ww.y - kcx.mul((T)kk * vv.y));
+                    };
+                    if (c == 0) {
+                        const C q0 = q(w, v, kyf * kyf), qN = q(P2[ky * NC + M], vN, M * M + kyf * kyf);
+                        S[ky * pitch + M] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
+                    } else {
+                        S[ky * pitch + M + c] = q(w, v, c * c + kyf * kyf);
+                    }
                 }
             }
         }
         __syncthreads();
         // ---- y inverse (natural in, transposed out) on nf*M columns
-        fft_lines_NT<NY, true, NT, nf * M>(S, LinearLines{1}, pitch, twY);
+        fft_lines_NT<NY, true, NT, nf * M>(S, LinearLines{1}, pitch, twY, twYl);
         __syncthreads();
         // ---- x C2R: half-length pre-processing, then inverse M-point FFT per row
         const PairRows<NY, pitch, M> rows;
@@ -155,18 +165,18 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 const C xk = row[k], xk2 = row[k2];
                 {
                     const C e = cadd(xk, cconj(xk2));
-                    const C o = cmulc(csub(xk, cconj(xk2)), twN[k]);  // * W_N^{-k}
+                    const C o = twmul<true>(csub(xk, cconj(xk2)), twN, twNl, k);  // * W_N^{-k}
                     row[k] = cmk<C>(e.x - o.y, e.y + o.x);            // e + i o
                 }
                 if (k2 != k) {
                     const C e = cadd(xk2, cconj(xk));
-                    const C o = cmulc(csub(xk2, cconj(xk)), twN[k2]);
+                    const C o = twmul<true>(csub(xk2, cconj(xk)), twN, twNl, k2);
                     row[k2] = cmk<C>(e.x - o.y, e.y + o.x);
                 }
             }
         }
         __syncthreads();
-        fft_lines_NT<M, true, NT, nf * NY>(S, rows, 1, twM);
+        fft_lines_NT<M, true, NT, nf * NY>(S, rows, 1, twM, twMl);
         __syncthreads();
 
         if (a.mode == XY_INV_PLAIN) {
@@ -181,25 +191,12 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
 
         // ---- pointwise over all slots (order-free)
         const PC<T> k(p);
-        const T eps = k.eps, ieps = k.ieps, ieps2 = k.ieps2, ieps3 = k.ieps3;
         if (a.mode == XY_NONLIN) {
-            // lambda_1 = M1 (V - alpha), lambda_2 = M2 (S - beta) (belastic.cpp:478-479),
-            // formed once per CTA in FP64 and broadcast in the kernel's precision
+            // lambdas formed once per CTA in FP64, broadcast in the kernel's precision
             T* lam = reinterpret_cast<T*>(red);
             const bool euler = p.method == M_EULER;
-            if (tid == 0) {
-                const Scal& sc = ctrl->sc[a.role];
-                const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
-                lam[0] = euler ? (T)(0.5 * lam1) : (T)(-0.5 * lam1);
-                lam[1] = euler ? (T)lam2 : (T)(-lam2 * 1.0606601717798212866);  // 3 / (2 sqrt 2)
-            }
+            if (tid == 0) nonlin_lambdas<T>(p, ctrl, a.role, lam);
             __syncthreads();
-            const T eta = k.eta;
-            const T kappa = (T)2.0, D = (T)1.5;  // phasefield.cpp:259-260
-            // ETD  (Calc.cu:428-437 with nld from :265-284):
-            //   G = -lam1/2 - c3 lam2 f - eta (D t / eps^3 + (3u^2 - D - 1) f / eps^2),  H = t
-            // Euler (Calc.cu:410-419 with g0 from :171-180):
-            //   G = lam1/2 + lam2 f + eta (3u^2 - 1) f / eps^2,                         H = f
             const T g_c = lam[0];
             const T g_f = lam[1];
             for (int it = tid; it < NY * M; it += NT) {
@@ -207,23 +204,11 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 C* pu = S + r * pitch + q;
                 C* pl = pu + M;
                 const C uu = *pu, ll = *pl;
-                T gv[2], hv[2];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const T u = e ? uu.y : uu.x, lap = e ? ll.y : ll.x;
-                    const T u2 = u * u;
-                    const T f = -lap * eps + (u2 - (T)1) * u * ieps;
-                    if (euler) {
-                        gv[e] = g_c + g_f * f + eta * ((T)3 * u2 - (T)1) * f * ieps2;
-                        hv[e] = f;
-                    } else {
-                        const T t = u * (u2 - (T)1 - kappa);
-                        gv[e] = g_c + g_f * f - eta * (D * t * ieps3 + ((T)3 * u2 - D - (T)1) * ieps2 * f);
-                        hv[e] = t;
-                    }
-                }
-                *pu = cmk<C>(gv[0], gv[1]);
-                *pl = cmk<C>(hv[0], hv[1]);
+                C g, h;
+                nonlin_point<T>(k, euler, g_c, g_f, uu.x, ll.x, g.x, h.x);
+                nonlin_point<T>(k, euler, g_c, g_f, uu.y, ll.y, g.y, h.y);
+                *pu = g;
+                *pl = h;
             }
             __syncthreads();
         } else {
@@ -234,18 +219,8 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 const int q = it % M, r = it / M;
                 const C uu = S[r * pitch + q];
                 const C ll = full ? S[r * pitch + M + q] : cmk<C>(0, 0);
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const T u = e ? uu.y : uu.x;
-                    const T u2m = u * u - (T)1;
-                    au.add(u);
-                    as.add(u2m * u2m);
-                    if (full) {
-                        const T lap = e ? ll.y : ll.x;
-                        const T f = -lap * eps + u2m * u * ieps;
-                        af.add(f * f);
-                    }
-                }
+                reduce_point<T>(k, full, uu.x, ll.x, au, as, af);
+                reduce_point<T>(k, full, uu.y, ll.y, au, as, af);
             }
             auto pv = au.part();
             decltype(pv) vv[3] = {pv, as.part(), af.part()};
@@ -279,7 +254,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     // ---- forward xy: x R2C (transposed in, natural out) then y (transposed in, natural out)
     constexpr int nfo = NF;  // XY_NONLIN (2 fields) or XY_FWD_PLAIN (1)
     const PairRows<NY, pitch, M> rows;
-    fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM);
+    fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl);
     __syncthreads();
     for (int it = tid; it < nfo * NY * (M / 2 + 1); it += NT) {
         const int l = it % (nfo * NY), k = it / (nfo * NY);
@@ -293,18 +268,18 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             const T h = (T)0.5;
             {
                 const C e = cadd(zk, cconj(zk2));
-                const C d = cmul(csub(zk, cconj(zk2)), twN[k]);
+                const C d = twmul<false>(csub(zk, cconj(zk2)), twN, twNl, k);
                 row[k] = cmk<C>(h * (e.x + d.y), h * (e.y - d.x));  // (e - i d) / 2
             }
             if (k2 != k) {
                 const C e = cadd(zk2, cconj(zk));
-                const C d = cmul(csub(zk2, cconj(zk)), twN[k2]);
+                const C d = twmul<false>(csub(zk2, cconj(zk)), twN, twNl, k2);
                 row[k2] = cmk<C>(h * (e.x + d.y), h * (e.y - d.x));
             }
         }
     }
     __syncthreads();
-    fft_lines_TN<NY, false, NT, nfo * M>(S, LinearLines{1}, pitch, twY);
+    fft_lines_TN<NY, false, NT, nfo * M>(S, LinearLines{1}, pitch, twY, twYl);
     __syncthreads();
 
     // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
@@ -316,7 +291,16 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     } else {
         outA = reinterpret_cast<C*>(a.cout) + (size_t)z * plane;
     }
-    const T bnl = PC<T>(p).bnl;
+    const PC<T> kst(p);
+    // g + beta cx |k_xy|^2 h: FP64 as the reference; FP32 with beta cx folded hi + lo
+    auto add_bnl = [&](C g, C hh, int kk) {
+        if constexpr (sizeof(T) == 8) {
+            const T mm = kst.bnl * (T)kk;
+            return cmk<C>(g.x + mm * hh.x, g.y + mm * hh.y);
+        } else {
+            return cmk<C>(g.x + kst.k_bnl.mul((T)kk * hh.x), g.y + kst.k_bnl.mul((T)kk * hh.y));
+        }
+    };
     for (int it = tid; it < NY * M; it += NT) {
         const int c = it % M, ky = it / M;
         const C zg = S[ky * pitch + c];
@@ -331,9 +315,8 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 const C zh = S[ky * pitch + M], zh2 = S[kym * pitch + M];
                 const C h0 = cmk<C>(h * (zh.x + zh2.x), h * (zh.y - zh2.y));
                 const C hN = cmk<C>(h * (zh.y + zh2.y), h * (zh2.x - zh.x));
-                const T m0 = bnl * (T)(kyf * kyf), mN = bnl * (T)(M * M + kyf * kyf);
-                outA[ky * NC] = cmk<C>(g0.x + m0 * h0.x, g0.y + m0 * h0.y);
-                outA[ky * NC + M] = cmk<C>(gN.x + mN * hN.x, gN.y + mN * hN.y);
+                outA[ky * NC] = add_bnl(g0, h0, kyf * kyf);
+                outA[ky * NC + M] = add_bnl(gN, hN, M * M + kyf * kyf);
                 outB[ky * NC] = h0;
                 outB[ky * NC + M] = hN;
             } else {
@@ -343,8 +326,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         } else {
             if (outB) {
                 const C zh = S[ky * pitch + M + c];
-                const T mm = bnl * (T)(c * c + kyf * kyf);
-                outA[ky * NC + c] = cmk<C>(zg.x + mm * zh.x, zg.y + mm * zh.y);
+                outA[ky * NC + c] = add_bnl(zg, zh, c * c + kyf * kyf);
                 outB[ky * NC + c] = zh;
             } else {
                 outA[ky * NC + c] = zg;
@@ -354,7 +336,9 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
 }
 
 template <class T, int NX> constexpr size_t xy_smem_bytes(int nf) {
-    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + NX / 2 + NX + NX) + (32 * 4 + 2) * sizeof(double);
+    constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
+    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + ntw * (NX / 2 + NX + NX)) +
+           (32 * 4 + 2) * sizeof(double);
 }
 
 }  // namespace cb

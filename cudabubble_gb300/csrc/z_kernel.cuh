@@ -96,6 +96,10 @@ template <> struct State<float> {
         df_add(r.hi.y, r.lo.y, incr.y);
         return r;
     }
+    // this - o, rounded once to FP32 (a stage increment: small next to either state)
+    __device__ __forceinline__ float2 diff(const State& o) const {
+        return make_float2((hi.x - o.hi.x) + (lo.x - o.lo.x), (hi.y - o.hi.y) + (lo.y - o.lo.y));
+    }
     // w |u|^2 with u = hi + lo: hi^2 exactly via FMA, the rest in a second sum
     template <class A> __device__ __forceinline__ void norm2_into(A& big, A& small, float w) const {
         const float px = hi.x * hi.x, py = hi.y * hi.y;
@@ -124,8 +128,10 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
     constexpr int W = 2 * TX;  // row pitch: field 0 in [0, TX), field 1 in [TX, 2 TX)
     C* S = reinterpret_cast<C*>(smem_raw);
     C* tw = S + NZ * W;
-    double* red = reinterpret_cast<double*>(tw + NZ);
-    for (int i = tid; i < NZ; i += NT) tw[i] = reinterpret_cast<const C*>(I.twz)[i];
+    constexpr int ntw = sizeof(T) == 4 ? 2 : 1;  // FP32: hi table then lo table
+    C* twl = tw + NZ;
+    double* red = reinterpret_cast<double*>(tw + ntw * NZ);
+    for (int i = tid; i < ntw * NZ; i += NT) tw[i] = reinterpret_cast<const C*>(I.twz)[i];
 
     const bool stage1 = a.mode == Z_ETD2_S1 || a.mode == Z_ETD4_S1 || a.mode == Z_EULER;
     const bool reuse = stage1 && !ctrl->fresh;  // retry of a rejected step: N_u / R-hat unchanged
@@ -146,8 +152,8 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             S[zz * W + TX + c] = vb;
         }
         __syncthreads();
-        if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw);
-        else fft_lines_NT<NZ, false, NT, TX>(S, LinearLines{1}, W, tw);
+        if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw, twl);
+        else fft_lines_NT<NZ, false, NT, TX>(S, LinearLines{1}, W, tw, twl);
         __syncthreads();
     }
 
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             if (m >= Mc) continue;
             const int kz = tidx<NZ>(r);
             const C v = S[r * W + c];
-            const C o = cmk<C>(v.x * invN, v.y * invN);
+            const C o = cmk<C>(k.k_invN.mul(v.x), k.k_invN.mul(v.y));
             if (to_state) State<T>::from(o).store(a.cout, (size_t)kz * Mc + m);
             else out[(size_t)kz * Mc + m] = o;
         }
@@ -205,14 +211,85 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
         C nh = cmk<C>(0, 0);
         if (need_fwd) {
             const C va = S[r * W + c], vb = S[r * W + TX + c];
-            const T mz = bnl * (T)(kzf * kzf);
-            nh = cmk<C>((va.x + mz * vb.x) * invN, (va.y + mz * vb.y) * invN);
+            if constexpr (sizeof(T) == 8) {
+                const T mz = bnl * (T)(kzf * kzf);
+                nh = cmk<C>((va.x + mz * vb.x) * invN, (va.y + mz * vb.y) * invN);
+            } else {  // beta cx and 1/N folded hi + lo: no systematic gain on N-hat
+                const T kk = (T)(kzf * kzf);
+                nh = cmk<C>(k.k_invN.mul(va.x + k.k_bnl.mul(kk * vb.x)), k.k_invN.mul(va.y + k.k_bnl.mul(kk * vb.y)));
+            }
         }
         const T* cf = coef + 8 * (kxy + kzf * kzf);
         State<T> us;           // the new stage / state spectrum
         bool have_state = true;
         C un;
-        switch (a.mode) {
+        if constexpr (sizeof(T) == 4) {
+            // FP32 form: N-hat = N'-hat + c_lin u-hat (misc_kernels.cuh, lin_coef).  nh is
+            // N'-hat; the c_lin terms act on the exact double-float spectra through the
+            // table, written with the stage increments d_a = a - phi, d_b = b - phi.
+            switch (a.mode) {
+                case Z_ETD2_S1:
+                case Z_ETD4_S1: {  // a = phi (+) (em' phi + c1 N'_u)
+                    if (reuse) nh = Nu[g]; else Nu[g] = nh;
+                    us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
+                    us.store(ah, g);
+                    break;
+                }
+                case Z_ETD2_S2: {  // phi' = a (+) (c2 (N'_a - N'_u) + c2 c_lin d_a)
+                    const C nu = Nu[g];
+                    const State<T> sa = State<T>::load(ah, g);
+                    const float2 da = sa.diff(State<T>::load(phat, g));
+                    us = sa.add(cmk<C>(fmaf(cf[3], da.x, cf[2] * (nh.x - nu.x)), fmaf(cf[3], da.y, cf[2] * (nh.y - nu.y))));
+                    us.store(cand, g);
+                    break;
+                }
+                case Z_ETD4_S2:
+                case Z_ETD4_S3:
+                case Z_ETD4_S4: {
+                    const State<T> sp = State<T>::load(phat, g), sa = State<T>::load(ah, g);
+                    const float2 da = sa.diff(sp);
+                    const T emh = cf[0], ch = cf[1], chcl = cf[6];
+                    // increment of b = phi (+) (em'_h phi + c_h N'_a + c_h c_lin d_a)
+                    auto inc_b = [&](C na) {
+                        return cmk<C>(fmaf(chcl, da.x, ch * na.x), fmaf(chcl, da.y, ch * na.y));
+                    };
+                    if (a.mode == Z_ETD4_S2) {
+                        Na[g] = nh;
+                        us = sp.axpy(emh, inc_b(nh));
+                        break;
+                    }
+                    const C na = Na[g], nu = Nu[g];
+                    const C ib = inc_b(na);
+                    const float2 db = make_float2(fmaf(emh, sp.hi.x, ib.x), fmaf(emh, sp.hi.y, ib.y));
+                    // increment of c = a (+) (em'_h a + c_h (2 N'_b - N'_u) + c_h c_lin (2 d_b - d_a))
+                    auto inc_c = [&](C nb) {
+                        return cmk<C>(fmaf(chcl, (T)2 * db.x - da.x, ch * ((T)2 * nb.x - nu.x)),
+                                      fmaf(chcl, (T)2 * db.y - da.y, ch * ((T)2 * nb.y - nu.y)));
+                    };
+                    if (a.mode == Z_ETD4_S3) {
+                        Nb[g] = nh;
+                        us = sa.axpy(emh, inc_c(nh));
+                        break;
+                    }
+                    // phi' = phi (+) (em'_4 phi + f1 N'_1 + f2 (N'_a + N'_b) + f3 N'_c
+                    //                 + c_lin (f1 d_1 + f2 (d_a + d_b) + f3 d_c))
+                    const C nb = Nb[g];
+                    const C ic = inc_c(nb);
+                    const float2 dc = make_float2(da.x + fmaf(emh, sa.hi.x, ic.x), da.y + fmaf(emh, sa.hi.y, ic.y));
+                    const T f1 = cf[3], f2 = cf[4], f3 = cf[5], cl = cf[7];
+                    const C n1 = ref4 ? na : nu;
+                    const float2 d1 = ref4 ? da : make_float2(0.f, 0.f);
+                    const C inc = cmk<C>(
+                        fmaf(cl, f1 * d1.x + f2 * (da.x + db.x) + f3 * dc.x, f1 * n1.x + f2 * (na.x + nb.x) + f3 * nh.x),
+                        fmaf(cl, f1 * d1.y + f2 * (da.y + db.y) + f3 * dc.y, f1 * n1.y + f2 * (na.y + nb.y) + f3 * nh.y));
+                    us = sp.axpy(cf[2], inc);
+                    us.store(cand, g);
+                    break;
+                }
+                default: break;
+            }
+        }
+        switch (sizeof(T) == 4 && a.mode <= Z_ETD4_S4 ? -1 : a.mode) {
             case Z_ETD2_S1: {  // a = e phi + c1 N_u (Calc.cu:453-455)
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
                 us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
@@ -243,15 +320,17 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
                     cf[0], cmk<C>(cf[1] * ((T)2 * nh.x - nu.x), cf[1] * ((T)2 * nh.y - nu.y)));
                 break;
             }
-            case Z_ETD4_S4: {  // e2 phi + f1 N1 + f2 (N1 + N_b) + f3 N_c (Calc.cu:556-567)
+            case Z_ETD4_S4: {  // e2 phi + f1 N1 + f2 (N_a + N_b) + f3 N_c (Calc.cu:556-567)
+                // N1 = N_a in the reference (belastic.cpp:550), N_u in Cox-Matthews
                 const T f1 = cf[3], f2 = cf[4], f3 = cf[5];
-                const C n1 = ref4 ? Na[g] : Nu[g], nb = Nb[g];
-                const C inc = cmk<C>(f1 * n1.x + f2 * (n1.x + nb.x) + f3 * nh.x,
-                                     f1 * n1.y + f2 * (n1.y + nb.y) + f3 * nh.y);
+                const C na = Na[g], n1 = ref4 ? na : Nu[g], nb = Nb[g];
+                const C inc = cmk<C>(f1 * n1.x + f2 * (na.x + nb.x) + f3 * nh.x,
+                                     f1 * n1.y + f2 * (na.y + nb.y) + f3 * nh.y);
                 us = State<T>::load(phat, g).axpy(cf[2], inc);
                 us.store(cand, g);
                 break;
             }
+            case -1: break;  // FP32 ETD stages, above
             case Z_EULER: {  // phi' = phi - dt ga R (Calc.cu:393-402)
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
                 us = State<T>::load(phat, g).add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
@@ -268,8 +347,13 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
                 const C v = (a.state_io & IO_CIN_STATE) ? State<T>::load(a.cin, g).work()
                                                         : reinterpret_cast<const C*>(a.cin)[g];
                 if (a.mul == SM_LAP) {
-                    const T mm = -cx * (T)(kx * kx + kyf * kyf + kzf * kzf);
-                    un = cmk<C>(mm * v.x, mm * v.y);
+                    const int kk = kx * kx + kyf * kyf + kzf * kzf;
+                    if constexpr (sizeof(T) == 8) {
+                        const T mm = -cx * (T)kk;
+                        un = cmk<C>(mm * v.x, mm * v.y);
+                    } else {
+                        un = cmk<C>(-k.k_cx.mul((T)kk * v.x), -k.k_cx.mul((T)kk * v.y));
+                    }
                 } else if (a.mul >= SM_DX) {
                     const T sq = sqrt(cx);
                     int kk;
@@ -294,14 +378,19 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
             // volume from the k = 0 mode: mean u = Re u-hat(0), exactly
             if (m == 0 && kz == 0) ctrl->sc[a.role].sum_u = us.re_exact() * (double)p.N;
         }
-        const T mz = -cx * (T)(kzf * kzf);
         S[r * W + c] = un;
-        S[r * W + TX + c] = cmk<C>(mz * un.x, mz * un.y);
+        if constexpr (sizeof(T) == 8) {
+            const T mz = -cx * (T)(kzf * kzf);
+            S[r * W + TX + c] = cmk<C>(mz * un.x, mz * un.y);
+        } else {
+            const T kk = (T)(kzf * kzf);
+            S[r * W + TX + c] = cmk<C>(-k.k_cx.mul(kk * un.x), -k.k_cx.mul(kk * un.y));
+        }
     }
     __syncthreads();
     const bool two = a.mode != Z_INV_PLAIN;
-    if (two) fft_lines_TN<NZ, true, NT, W>(S, LinearLines{1}, W, tw);
-    else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw);
+    if (two) fft_lines_TN<NZ, true, NT, W>(S, LinearLines{1}, W, tw, twl);
+    else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw, twl);
     __syncthreads();
 
     // ---- store partials (natural z)
@@ -352,7 +441,8 @@ __global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ inst
 }
 
 template <class T, int NZ, int TX> constexpr size_t z_smem_bytes() {
-    return sizeof(cplx<T>) * ((size_t)NZ * 2 * TX + NZ) + (32 * 2 + 2) * sizeof(double);
+    constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
+    return sizeof(cplx<T>) * ((size_t)NZ * 2 * TX + ntw * NZ) + (32 * 2 + 2) * sizeof(double);
 }
 
 }  // namespace cb

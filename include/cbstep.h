@@ -92,6 +92,9 @@ typedef struct cb_params {
     int accurate_coefficients; /* -1: default (FP32 form: phi-function series; FP64 form: reference closed forms) */
     double rel_tol;          /* > 0: cb_run stops (CB_DONE_CONVERGED) once an accepted step changes
                                 E by less than rel_tol |E|; not in the reference loops */
+    int xy_split;            /* 1: always use the split (y-column + x-row) plane passes; 0: only where
+                                a plane's two fields do not fit one CTA (FP64 from 128^2, all 192^2+) */
+    int pad0;
 } cb_params;
 
 typedef struct cb_scalars {

@@ -346,6 +346,8 @@ static void etd4_step(cstep* h, int textbook) {  /* belastic.cpp:519-552 */
     }
     c2r(&h->F, ch, ar, h->ctmp);
     nld_term(h, ar, fa, bb); /* bb = nldc */
+    /* the reference passes nlda in the first slot too (belastic.cpp:550);
+       Cox-Matthews has N_u there: f1 N_u + f2 (N_a + N_b) + f3 N_c */
     const cx* n1 = textbook ? nl : nla;
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)Nc; ++i) {  /* etd44 */
@@ -354,8 +356,8 @@ static void etd4_step(cstep* h, int textbook) {  /* belastic.cpp:519-552 */
         const double a1 = -4.0 - hh * L + e2 * (4.0 - 3.0 * hh * L + hh * hh * L * L);
         const double a2 = 2.0 + hh * L + e2 * (-2 + hh * L);
         const double a3 = -4 - 3 * hh * L - hh * hh * L * L + e2 * (4 - hh * L);
-        ch[i].re = e2 * fd[i].re + q * (n1[i].re * a1 + 2 * (n1[i].re + nlb[i].re) * a2 + bb[i].re * a3);
-        ch[i].im = e2 * fd[i].im + q * (n1[i].im * a1 + 2 * (n1[i].im + nlb[i].im) * a2 + bb[i].im * a3);
+        ch[i].re = e2 * fd[i].re + q * (n1[i].re * a1 + 2 * (nla[i].re + nlb[i].re) * a2 + bb[i].re * a3);
+        ch[i].im = e2 * fd[i].im + q * (n1[i].im * a1 + 2 * (nla[i].im + nlb[i].im) * a2 + bb[i].im * a3);
     }
     c2r(&h->F, ch, h->d, h->ctmp);
     free(ch);

@@ -170,14 +170,14 @@ class Calc:
 
     # Calc.cu:549-577 etd44_kernel (first slot receives whatever the caller passes)
     @staticmethod
-    def etd44(fd, n1, nldb, nldc, Het, dt):
+    def etd44(fd, n1, nlda, nldb, nldc, Het, dt):
         e1 = np.exp(Het * dt / 2.0)
         e2 = e1 * e1
         h = dt
         L = Het
         return e2 * fd + 1.0 / (h * h * L * L * L) * (
             n1 * (-4.0 - h * L + e2 * (4.0 - 3.0 * h * L + h * h * L * L))
-            + 2.0 * (n1 + nldb) * (2.0 + h * L + e2 * (-2.0 + h * L))
+            + 2.0 * (nlda + nldb) * (2.0 + h * L + e2 * (-2.0 + h * L))
             + nldc * (-4.0 - 3.0 * h * L - h * h * L * L + e2 * (4.0 - h * L)))
 
 
@@ -405,11 +405,13 @@ class Belastic:
         chat = half(chat, 2.0 * nldb - nld) if acc else c.etd43(chat, nld, nldb, L, dt)
         self.pa.update_fd(chat)
         nldc = self.get_nld_term(self.pa)
+        # the reference passes nlda in the first slot (belastic.cpp:550); Cox-Matthews
+        # has N_u there: f1 N_u + f2 (N_a + N_b) + f3 N_c
         first = nlda if self.p.etd4_reference_combine else nld
         if acc:
-            d = np.exp(L * dt) * self.pd.fd() + f1 * first + f2 * (first + nldb) + f3 * nldc
+            d = np.exp(L * dt) * self.pd.fd() + f1 * first + f2 * (nlda + nldb) + f3 * nldc
         else:
-            d = c.etd44(self.pd.fd(), first, nldb, nldc, L, dt)
+            d = c.etd44(self.pd.fd(), first, nlda, nldb, nldc, L, dt)
         self.pd.d = c.c2r_3d_b(d)
         self.pd.update_d()
 
