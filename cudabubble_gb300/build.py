@@ -30,10 +30,19 @@ def nvcc() -> str:
     return exe
 
 
+STAMP = os.path.join(LIBDIR, "build_defines.txt")
+
+
+def defines() -> list[str]:
+    """Extra -D flags from CB_NVCC_DEFINES (launch-shape tuning, e.g.
+    -DCB_XY_NT_LARGE=1024); the library is rebuilt whenever they change."""
+    return [d for d in os.environ.get("CB_NVCC_DEFINES", "").split() if d.startswith("-D")]
+
+
 def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
     cmd = [nvcc(), "-std=c++17", *ARCH, "-lineinfo", "-O3", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
-           "-c", os.path.join(CSRC, src), "-o", obj]
+           *defines(), "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}")
@@ -42,6 +51,9 @@ def _compile(src: str) -> str:
 
 def _stale() -> bool:
     if not os.path.exists(LIB):
+        return True
+    old = open(STAMP).read() if os.path.exists(STAMP) else ""
+    if old != " ".join(defines()):
         return True
     t = os.path.getmtime(LIB)
     for d in (CSRC, INCLUDE, PKG):
@@ -66,6 +78,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(" ".join(defines()))
     if verbose:
         print("built", LIB)
     return LIB

@@ -85,6 +85,7 @@ struct Params {
     double grow_factor, dt_cap, cap_probe, dt_min;
     double tmax;        // Euler loop time limit (belastic.cpp:407)
     double rel_tol;     // > 0: stop once an accepted step changes E by < rel_tol |E|
+    double reject_tol;  // adaptive: reject when E_new > E_old + reject_tol |E_old|
     // host-precomputed constants: GB300 runs FP64 at a small fraction of its
     // FP32 rate, so kernels read these instead of dividing per thread
     double d_ieps, d_ieps2, d_ieps3, d_bnl;  // 1/eps, 1/eps^2, 1/eps^3, beta * cx

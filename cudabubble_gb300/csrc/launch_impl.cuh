@@ -13,15 +13,25 @@ namespace cb {
 
 constexpr size_t kMaxSmem = 227 * 1024;
 
+// threads of the single-CTA xy pass for planes of 96^2 and 128^2: the
+// nonlinear pass (two fields both ways) gains from 32 warps per plane, the
+// reductions (inverse only) do not (build-time knobs, measured on GB300)
+#ifndef CB_XY_NT_LARGE
+#define CB_XY_NT_LARGE 512
+#endif
+#ifndef CB_XY_NT_NONLIN
+#define CB_XY_NT_NONLIN 1024
+#endif
+
 template <class T, int NX> struct XYCfg {
-    static constexpr int NT = NX <= 32 ? 128 : (NX <= 64 ? 256 : 512);
+    static constexpr int NT = NX <= 32 ? 128 : (NX <= 64 ? 256 : CB_XY_NT_LARGE);
+    static constexpr int NT_NONLIN = NX <= 64 ? NT : CB_XY_NT_NONLIN;
     static constexpr bool ok = xy_smem_bytes<T, NX>(2) <= kMaxSmem;   // stepping (two fields)
     static constexpr bool ok1 = xy_smem_bytes<T, NX>(1) <= kMaxSmem;  // plain transforms (one field)
 };
 
-template <class T, int NX, int NF>
+template <class T, int NX, int NF, int NT>
 static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
-    constexpr int NT = XYCfg<T, NX>::NT;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -37,10 +47,11 @@ template <class T, int NX>
 static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
     const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN;
     if constexpr (XYCfg<T, NX>::ok) {
-        if (two) return xy_go_nf<T, NX, 2>(d, ninst, nzmax, a, s);
+        if (a.mode == XY_NONLIN) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN>(d, ninst, nzmax, a, s);
+        if (two) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT>(d, ninst, nzmax, a, s);
     }
     if constexpr (XYCfg<T, NX>::ok1) {
-        if (!two) return xy_go_nf<T, NX, 1>(d, ninst, nzmax, a, s);
+        if (!two) return xy_go_nf<T, NX, 1, XYCfg<T, NX>::NT>(d, ninst, nzmax, a, s);
     }
     return cudaErrorInvalidValue;
 }

@@ -185,7 +185,7 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     c->E_last_attempt = E1;
     if (!raw) {
         if (p.adaptive) {
-            if (E1 > c->E_state) {
+            if (E1 > c->E_state + p.reject_tol * fabs(c->E_state)) {
                 c->dt *= 0.5;
                 c->rejects++;
                 c->fresh = 0;

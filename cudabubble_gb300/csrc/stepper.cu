@@ -25,6 +25,7 @@ void cb_params_default(cb_params* p) {
     p->method = CB_ETD4;
     p->precision = CB_FP64;
     p->accurate_coefficients = -1;
+    p->reject_tol = -1.0;
 }
 
 int cb_params_from_ini_line(const char* line, cb_params* p) {

@@ -151,6 +151,11 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.dt_min = 1e-23;
     p.tmax = u.tmax >= 0 ? u.tmax : 4.0;
     p.rel_tol = u.rel_tol > 0 ? u.rel_tol : 0.0;
+    // the FP32 form's step-to-step energy changes carry FP32 transform noise of up to
+    // ~5e-6 relative late in a relaxation (high-|k| modes re-seeded each step); a rise
+    // below that is not one it can resolve, and rejecting on it halves dt on noise
+    // alone until dt underflows
+    p.reject_tol = u.reject_tol >= 0 ? u.reject_tol : (u.precision == CB_FP32 ? 1e-5 : 0.0);
     // nonlinear term N-hat = A-hat + beta cx |k|^2 B-hat: beta = eta (Euler, -lap f in g0)
     // or -eta/eps (ETD, +lap t / eps in -eta NL)
     const double beta = euler ? p.eta : -p.eta / p.eps;

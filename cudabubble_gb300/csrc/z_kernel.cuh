@@ -111,7 +111,7 @@ template <> struct State<float> {
 };
 
 template <class T, int NZ, int TX, int NT>
-__global__ void __launch_bounds__(NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+__global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const InstT<T>& I = insts[blockIdx.y];
