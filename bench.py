@@ -11,9 +11,19 @@ the stepper's stream and L2 is flushed (256 MiB memset) between attempts,
 outside the timed events.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--no-cpu-baseline] [--no-extra]
 
 --impl reference times the reference algorithm's CPU form (oracle/cstep.c,
 the plain FP64 C port with OpenMP on every host core) on the same workload.
+
+Besides the headline line's keys, the JSON carries (unless --no-extra):
+  plain_fp64  the plain FP64 form of this stepper on the same workload (the
+              "vs plain FP64" of the metric), and the FP32 form's speed-up;
+  batched     workload config 4: 64 vesicles of grids drawn from
+              {32,48,64,96,128}^3 advanced together (cb_batch_*);
+  served      workload config 5: a Poisson trace at 200 req/s of relaxations
+              on grids {32..256}^3 through the continuous-batching server
+              (cb_serve_trace), with p50/p99 latency.
 """
 from __future__ import annotations
 
@@ -152,14 +162,74 @@ def algorithmic_bytes(n: int, fsize: int, att: int, rej: int):
     state fields (phi-hat, candidate, a-hat) are double-float pairs, 2F."""
     F = n * n * (n // 2 + 1) * 2 * fsize
     return {
-        "xy_nonlin": (2 * att - rej) * 4 * F,          # read P0, P2; write A, B
-        "xy_reduce_s": att * 1 * F,                     # read P0
-        "xy_reduce_full": att * 2 * F,                  # read P0, P2
-        # S2: read A, B, a-hat(2F), N_u; write phi'(2F), P0, P2          = 9F
-        # S1 fresh: read A, B, phi(2F); write N_u, a-hat(2F), P0, P2     = 9F
+        "xy_fused": att * 2 * 4 * F,                    # per stage: read P0, P2; write G'', w
+        # S2: read A, B, a-hat(2F), phi(2F), N_u; write phi'(2F), P0, P2 = 11F
+        # S1 fresh: read G'', w, phi(2F); write N_u, a-hat(2F), P0, P2   = 9F
         # S1 retry: read N_u, phi(2F); write a-hat(2F), P0, P2           = 7F
-        "z_stage": att * 9 * F + (att - rej) * 9 * F + rej * 7 * F,
+        "z_stage": att * 11 * F + (att - rej) * 9 * F + rej * 7 * F,
     }, F
+
+
+# launches of one ETD-RK2 attempt of the FP32 form: prologue, coefficient fill,
+# z S1, xy FUSED (work), z S2, xy FUSED (candidate), decide
+LAUNCHES_PER_ATTEMPT = 7
+
+
+def plain_fp64(steps: int):
+    """The plain FP64 form of this stepper on the headline workload (same
+    timing and L2 flushing as the FP32 line)."""
+    from cudabubble_gb300 import capi
+    p = capi.default_params(nx=N_GRID, ny=N_GRID, nz=N_GRID, epssize=EPSSIZE, method=capi.CB_ETD2,
+                            precision=capi.CB_FP64, time_step=DT0, fixed_time_step=0.0, M1=1e4, M2=1e4)
+    st = capi.Stepper(p)
+    st.set_phi(phi0())
+    st.run(3)
+    st.set_phi(phi0())
+    r = st.run_timed(steps, FLUSH_BYTES)
+    sc = st.scalars()
+    st.close()
+    ms = r["device_ms"]
+    ref_E = golden_energy(sc["steps"])
+    return {"value": N_GRID ** 3 * sc["steps"] / (ms / 1e3), "unit": UNIT, "steps": sc["steps"],
+            "attempts": r["attempts"], "ms_per_step": ms / max(sc["steps"], 1),
+            "rel_E_error_vs_reference": abs(sc["E"] - ref_E) / abs(ref_E) if ref_E else None,
+            "what": "CB_FP64 (FP64 transforms, split y/x plane passes at 128^2), same workload, steps 1..K"}
+
+
+def batched(steps: int):
+    """Workload config 4 through cb_batch (FP32 form)."""
+    from cudabubble_gb300 import capi, workloads
+    plist, phis = workloads.batched()
+    b = capi.Batch(plist)
+    for i, ph in enumerate(phis):
+        b.set_phi(i, ph)
+    b.run(3)
+    for i, ph in enumerate(phis):
+        b.set_phi(i, ph)
+    r = b.run_timed(steps, FLUSH_BYTES)
+    pts = sum(p.nx * p.ny * p.nz * b.scalars(i)["steps"] for i, p in enumerate(plist))
+    b.close()
+    return {"value": pts / (r["device_ms"] / 1e3), "unit": UNIT, "instances": len(plist),
+            "grid_points": int(sum(p.nx * p.ny * p.nz for p in plist)), "steps_per_instance": steps,
+            "attempts": r["attempts"], "device_ms": r["device_ms"],
+            "what": "config 4: 64 vesicles, grids U{32,48,64,96,128}^3 (seed 4), alpha x U[0.6,0.95], ETD-RK2 "
+                    "per-instance adaptive dt, one CUDA graph per attempt over all size classes, FP32 form"}
+
+
+def served(duration_s: float, max_steps: int):
+    """Workload config 5 through cb_serve_trace (FP32 form, 150 GB budget)."""
+    from cudabubble_gb300 import capi, workloads
+    reqs = workloads.served(duration_s=duration_s, max_steps=max_steps)
+    res, stats, _ = capi.serve_trace(reqs, 150 * 10 ** 9, max_slots_per_class=64, quantum=4)
+    lat = np.array([r["latency_s"] for r in res])
+    conv = sum(1 for r in res if r["status"] == 5)
+    return {"requests": len(reqs), "completed": stats["completed"], "converged": conv,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "value": stats["point_steps"] / stats["wall_s"], "unit": UNIT, "wall_s": stats["wall_s"],
+            "peak_bytes": stats["peak_bytes"],
+            "what": f"config 5: Poisson 200 req/s for {duration_s:g} s (seed 5), grids {{32..256}}^3 weighted "
+                    f"30/25/20/15/7/3 %, ETD-RK2 to |dE/E|<1e-8 capped at {max_steps} steps, 150 GB budget, "
+                    "continuous batching, FP32 form; latency = finish - arrival"}
 
 
 def run_ours(args, rank: int, world: int):
@@ -256,7 +326,7 @@ def run_ours(args, rank: int, world: int):
                       "rejects": rejects, "l2": "flushed between attempts (256 MiB memset, outside timed events)",
                       "parallelism": "replicas" if world > 1 else "single GPU", "points": N},
            "accuracy": {"E_step_K": sc["E"], "E_reference_fp64_cufft": ref_E, "rel_E_error": rel_E},
-           "e2e": e2e, "gpu_launches": attempts * 8, "roofline": roofline,
+           "e2e": e2e, "gpu_launches": attempts * LAUNCHES_PER_ATTEMPT, "roofline": roofline,
            "wall_s_timed_region": wall}
     clk_sum = clk.summary()
     res["clocks"] = clk_sum
@@ -270,6 +340,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -297,6 +368,12 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     res = run_ours(args, rank, world)
+    if rank == 0 and not args.no_extra:
+        pf = plain_fp64(args.steps)
+        res["plain_fp64"] = pf
+        res["speedup_fp32_over_plain_fp64"] = res["value"] / pf["value"]
+        res["batched"] = batched(min(args.steps, 60))
+        res["served"] = served(2.0, 200)
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline()

@@ -226,11 +226,11 @@ class Stepper:
             check(rc)
         return {"device_ms": ms.value, "attempts": att.value, "rc": rc}
 
-    KERNEL_KINDS = ("xy_nonlin", "xy_reduce_s", "xy_reduce_full", "z_stage", "decide_coef")
+    KERNEL_KINDS = ("xy_nonlin", "xy_reduce_s", "xy_reduce_full", "z_stage", "decide_coef", "xy_fused")
 
     def profile_kernels(self, nattempts: int, flush_bytes: int = 0) -> dict:
-        ms = (C.c_double * 5)()
-        cnt = (C.c_int * 5)()
+        ms = (C.c_double * len(self.KERNEL_KINDS))()
+        cnt = (C.c_int * len(self.KERNEL_KINDS))()
         check(lib().cb_profile_kernels(self.h, nattempts, flush_bytes, ms, cnt))
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.KERNEL_KINDS)}
 

@@ -58,6 +58,7 @@ struct Ctrl {
     int corr_phase;   // alpha/beta correction sub-step (fixed dt, M != 0)
     int nonfinite;
     int grow_pending;  // apply the dt growth rule at the start of the next attempt
+    int ab_state;      // FP32 form: G[ab_state] holds the state's fused-pass outputs
     int tab_cur;       // coefficient table of the current dt
     int tab_next;      // round-robin slot for the next new dt
     int fill_slot;     // table being filled this attempt (-1: none)
@@ -131,6 +132,7 @@ template <class T> struct InstT {
     void* A;
     void* B;
     void* Y[2];       // split plane path: y-transformed fields (nullptr when unused)
+    void* G[2][2];    // FP32 form: XY_FUSED outputs (G'', w) of the state / candidate (ctrl->ab_state)
     T* coef;          // kNTab tables of (kmax + 1) * 8 entries
     Ctrl* ctrl;
     double* part_xy;  // [nz][4] per-plane partial sums

@@ -3,7 +3,10 @@
 
 namespace cb {
 
-enum XYMode { XY_REDUCE_FULL = 0, XY_REDUCE_S = 1, XY_NONLIN = 2, XY_INV_PLAIN = 3, XY_FWD_PLAIN = 4 };
+// XY_FUSED (FP32 form): the sums of XY_REDUCE_FULL and the lambda-free
+// nonlinear partials G'', w of the same state in one pass; the penalty terms
+// enter in the next z pass, once the sums have given lambda.
+enum XYMode { XY_REDUCE_FULL = 0, XY_REDUCE_S = 1, XY_NONLIN = 2, XY_FUSED = 3, XY_INV_PLAIN = 4, XY_FWD_PLAIN = 5 };
 
 struct XYArgs {
     int mode;
@@ -37,6 +40,8 @@ struct YArgs {
     int role;           // stepping: partial set read (inverse)
     int stepping;       // 1: instance buffers (P / Y / A, B) and the done / stale checks
     int skip_if_stale;
+    int fused;          // forward of an XY_FUSED pass: outputs go to the role's slot
+    int pad;
     const void* cin;    // plain inverse: partial C[nz][ny][nc]
     void* cout;         // plain forward: partial C[nz][ny][nc]
 };

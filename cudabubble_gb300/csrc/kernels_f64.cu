@@ -1,7 +1,7 @@
 // FP64 instantiation of the stepper kernels (the plain form) and the
-// precision-independent slow-path kernels.
+// precision-independent slow-path kernels (the z pass is in kernels_f64_z.cu).
 #include "launch_impl.cuh"
-template struct cb::Launch<double>;
+CB_INSTANTIATE_XY(double)
 
 namespace cb {
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,

@@ -1,0 +1,3 @@
+// FP64 instantiation of the z pass.
+#include "launch_impl.cuh"
+CB_INSTANTIATE_Z(double)

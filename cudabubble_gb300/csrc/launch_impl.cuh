@@ -45,9 +45,9 @@ static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArg
 
 template <class T, int NX>
 static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
-    const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN;
+    const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED;
     if constexpr (XYCfg<T, NX>::ok) {
-        if (a.mode == XY_NONLIN) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN>(d, ninst, nzmax, a, s);
+        if (a.mode == XY_NONLIN || a.mode == XY_FUSED) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN>(d, ninst, nzmax, a, s);
         if (two) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT>(d, ninst, nzmax, a, s);
     }
     if constexpr (XYCfg<T, NX>::ok1) {
@@ -99,11 +99,13 @@ static cudaError_t xy_split_go(const InstT<T>* d, int ninst, int nzmax, const XY
     YArgs y;
     memset(&y, 0, sizeof y);
     y.role = a.role;
-    y.stepping = a.mode <= XY_NONLIN;
+    y.stepping = a.mode <= XY_FUSED;
     y.skip_if_stale = a.skip_if_stale;
+    y.fused = a.mode == XY_FUSED;
     cudaError_t r = cudaSuccess;
     switch (a.mode) {
         case XY_NONLIN:
+        case XY_FUSED:
         case XY_REDUCE_FULL:
             y.mode = Y_INV2;
             break;
@@ -124,27 +126,38 @@ static cudaError_t xy_split_go(const InstT<T>* d, int ninst, int nzmax, const XY
     }
     r = xrow_go<T, NX>(d, ninst, nzmax, a, s);
     if (r != cudaSuccess) return r;
-    if (a.mode == XY_NONLIN || a.mode == XY_FWD_PLAIN) {
-        y.mode = a.mode == XY_NONLIN ? Y_FWD2 : Y_FWD1;
+    if (a.mode == XY_NONLIN || a.mode == XY_FUSED || a.mode == XY_FWD_PLAIN) {
+        y.mode = a.mode == XY_FWD_PLAIN ? Y_FWD1 : Y_FWD2;
         y.cout = a.cout;
         r = ycol_go<T, NX>(d, ninst, nzmax, y, s);
     }
     return r;
 }
 
-template <class T, int NZ>
-static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
+template <class T, int NZ, int MG>
+static cudaError_t z_go_g(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
     constexpr int TX = ztile<T>();
     constexpr int NT = 256;
     constexpr size_t sm = z_smem_bytes<T, NZ, TX>();
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(z_kernel<T, NZ, TX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t e =
+            cudaFuncSetAttribute(z_kernel<T, NZ, TX, NT, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    z_kernel<T, NZ, TX, NT><<<dim3(ntiles, ninst), NT, sm, s>>>(d, a);
+    z_kernel<T, NZ, TX, NT, MG><<<dim3(ntiles, ninst), NT, sm, s>>>(d, a);
     return cudaGetLastError();
+}
+
+template <class T, int NZ>
+static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
+    switch (zgroup_of(a.mode)) {
+        case ZG_ETD2: return z_go_g<T, NZ, ZG_ETD2>(d, ninst, ntiles, a, s);
+        case ZG_ETD4: return z_go_g<T, NZ, ZG_ETD4>(d, ninst, ntiles, a, s);
+        case ZG_EULER: return z_go_g<T, NZ, ZG_EULER>(d, ninst, ntiles, a, s);
+        default: return z_go_g<T, NZ, ZG_PLAIN>(d, ninst, ntiles, a, s);
+    }
 }
 
 #define CB_XY_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128)
@@ -182,7 +195,7 @@ template <class T> int Launch<T>::z_tile() { return ztile<T>(); }
 template <class T>
 cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
                           int split) {
-    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
+    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED) ? 2 : 1;
     if (!split && xy_single(nx, nf)) {
         switch (nx) {
 #define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s);
@@ -245,3 +258,23 @@ cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_
 }
 
 }  // namespace cb
+
+// explicit instantiation, split in two translation units per precision so the
+// z-pass instances (four mode groups x nine sizes) compile in parallel
+#define CB_INSTANTIATE_XY(T)                                                                                        \
+    template bool cb::Launch<T>::xy_supported(int);                                                                 \
+    template bool cb::Launch<T>::xy_plain_supported(int);                                                           \
+    template bool cb::Launch<T>::xy_single(int, int);                                                               \
+    template bool cb::Launch<T>::xy_split_supported(int);                                                           \
+    template int cb::Launch<T>::xy_rows_per_cta(int);                                                               \
+    template cudaError_t cb::Launch<T>::xy(int, const cb::InstT<T>*, int, int, const cb::XYArgs&, cudaStream_t, int); \
+    template cudaError_t cb::Launch<T>::decide(const cb::InstT<T>*, int, int, cudaStream_t);                        \
+    template cudaError_t cb::Launch<T>::coef(const cb::InstT<T>*, int, int, cudaStream_t, int);                    \
+    template cudaError_t cb::Launch<T>::to_double(const void*, double*, size_t, cudaStream_t);                     \
+    template cudaError_t cb::Launch<T>::nhat_full(const cb::InstT<T>*, const void*, double*, size_t, cudaStream_t); \
+    template cudaError_t cb::Launch<T>::state_to_double(const void*, double*, size_t, cudaStream_t);               \
+    template cudaError_t cb::Launch<T>::f64_to_state(const void*, void*, size_t, int, cudaStream_t);
+#define CB_INSTANTIATE_Z(T)                                    \
+    template bool cb::Launch<T>::z_supported(int);             \
+    template int cb::Launch<T>::z_tile();                      \
+    template cudaError_t cb::Launch<T>::z(int, const cb::InstT<T>*, int, int, const cb::ZArgs&, cudaStream_t);

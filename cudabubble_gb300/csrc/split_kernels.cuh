@@ -63,8 +63,7 @@ __global__ void __launch_bounds__(NT) ycol_kernel(const InstT<T>* __restrict__ i
         src0 = I.Y[0];
         src1 = I.Y[1];
         if (a.stepping) {
-            dst0 = I.A;
-            dst1 = I.B;
+            nl_outputs<T>(I, ctrl, a.fused ? XY_FUSED : XY_NONLIN, a.role, dst0, dst1);
         } else {
             dst0 = a.cout;
         }
@@ -151,12 +150,12 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
     const int nblk = nrows / RPC;
     const int rb = blockIdx.x;
     if (rb >= nblk) return;
-    const bool stepping = a.mode <= XY_NONLIN;
+    const bool stepping = a.mode <= XY_FUSED;
     if (stepping) {
         if (ctrl->done) return;
         if (a.skip_if_stale && !ctrl->fresh) return;
     }
-    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN) ? 2 : 1;
+    const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED) ? 2 : 1;
     constexpr int ntw = sizeof(T) == 4 ? 2 : 1;
     C* S = reinterpret_cast<C*>(smem_raw);  // line l = f * RPC + j: field f of row j
     C* twM = S + 2 * RPC * LP;
@@ -238,6 +237,26 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
                 *pl = h;
             }
             __syncthreads();
+        } else if (a.mode == XY_FUSED) {
+            const bool euler = p.method == M_EULER;
+            Acc<T> au, as, af;
+            for (int it = tid; it < RPC * M; it += NT) {
+                const int q = it % M, j = it / M;
+                C* pu = S + j * LP + q;
+                C* pl = S + (RPC + j) * LP + q;
+                const C uu = *pu, ll = *pl;
+                reduce_point<T>(k, true, uu.x, ll.x, au, as, af);
+                reduce_point<T>(k, true, uu.y, ll.y, au, as, af);
+                C g, h;
+                nonlin_point<T>(k, euler, (T)0, (T)0, uu.x, ll.x, g.x, h.x);
+                nonlin_point<T>(k, euler, (T)0, (T)0, uu.y, ll.y, g.y, h.y);
+                *pu = g;
+                *pl = h;
+            }
+            auto pv = au.part();
+            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            xy_sums_finalize<T>(I, ctrl, p, rb, nblk, vv, red, a.role, true);
+            __syncthreads();
         } else {
             const bool full = a.mode == XY_REDUCE_FULL;
             Acc<T> au, as, af;
@@ -250,36 +269,14 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
             }
             auto pv = au.part();
             decltype(pv) vv[3] = {pv, as.part(), af.part()};
-            double v[3];
-            block_sum<3>(vv, v, red);
-            double* part = I.part_xy;
-            int* last = reinterpret_cast<int*>(red + 128);
-            if (tid == 0) {
-                part[4 * rb + 0] = v[0];
-                part[4 * rb + 1] = v[1];
-                part[4 * rb + 2] = v[2];
-                part[4 * rb + 3] = 0.0;
-                __threadfence();
-                const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[a.role], 1u);
-                *last = done_blocks == (unsigned)(nblk - 1);
-            }
-            __syncthreads();
-            if (*last) {
-                __threadfence();
-                double sums[4];
-                block_sum_parts<4>(part, nblk, sums, red);
-                if (tid == 0) {
-                    finalize_xy(p, ctrl, sums, a.role, full);
-                    ctrl->cnt_xy[a.role] = 0u;
-                }
-            }
+            xy_sums_finalize<T>(I, ctrl, p, rb, nblk, vv, red, a.role, full);
             return;
         }
     }
 
     // ---- x R2C: forward M-point transform, then
     //      X[k] = (e - i d) / 2, e = Z[k] + conj Z[M-k], d = (Z[k] - conj Z[M-k]) W_N^k
-    const int nfo = a.mode == XY_NONLIN ? 2 : 1;
+    const int nfo = (a.mode == XY_NONLIN || a.mode == XY_FUSED) ? 2 : 1;
     if (nfo == 2) fft_lines_TN<M, false, NT, 2 * RPC>(S, lines, 1, twM, twMl);
     else fft_lines_TN<M, false, NT, RPC>(S, lines, 1, twM, twMl);
     __syncthreads();

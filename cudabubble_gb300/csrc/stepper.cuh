@@ -15,6 +15,12 @@
 //     -> xy REDUCE_FULL(cand) -> decide
 // The stage-1 nonlinear spectrum does not depend on dt, so a rejected attempt
 // reuses it (the xy NONLIN on the state is skipped while ctrl->fresh == 0).
+//
+// The FP32 form runs one xy pass per stage (XY_FUSED: the stage state's sums
+// and its lambda-free nonlinear partials together); the penalty terms enter
+// in the following z pass, which reads lambda from those sums:
+//   ETD-RK2  z ETD2_S1 -> xy FUSED(work) -> z ETD2_S2 -> xy FUSED(cand) -> decide
+// and the candidate's partials become the next state's (G slot swap on accept).
 #pragma once
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -204,7 +210,8 @@ struct Handle {
 };
 
 // kernel kinds reported by cb_profile_kernels
-enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, K_DECIDE = 4, K_NKIND = 5 };
+enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, K_DECIDE = 4, K_XY_FUSED = 5,
+       K_NKIND = 6 };
 
 // One attempt of the method's loop for `ninst` instances that share grid and
 // method (an instance table on the device), on stream s.  With prof set, an
@@ -226,7 +233,9 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
         prof->emplace_back(kind, a, b);
     };
     auto X = [&](int m, int role, int skip = 0) {
-        const int kind = m == XY_NONLIN ? K_XY_NONLIN : (m == XY_REDUCE_S ? K_XY_REDUCE_S : K_XY_REDUCE_FULL);
+        const int kind = m == XY_NONLIN ? K_XY_NONLIN
+                         : m == XY_FUSED ? K_XY_FUSED
+                         : (m == XY_REDUCE_S ? K_XY_REDUCE_S : K_XY_REDUCE_FULL);
         timed(kind, [&]() {
             XYArgs a;
             memset(&a, 0, sizeof a);
@@ -247,6 +256,33 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
     };
     // prologue: pending dt growth, coefficient table for the attempt's dt
     timed(K_DECIDE, [&]() { return Launch<T>::coef(d, ninst, accurate, s, raw ? 1 : 0); });
+    if (sizeof(T) == 4) {
+        // FP32 form: every xy pass is XY_FUSED (sums + lambda-free partials of the
+        // same state); stage 1 reads the state's outputs from its G slot, left by the
+        // candidate pass of the attempt that accepted it (or by cb_set_phi)
+        switch (method) {
+            case M_ETD2:
+                Z(Z_ETD2_S1, R_WORK);
+                X(XY_FUSED, R_WORK);
+                Z(Z_ETD2_S2, R_CAND);
+                X(XY_FUSED, R_CAND);
+                break;
+            case M_ETD4:
+                Z(Z_ETD4_S1, R_WORK);
+                X(XY_FUSED, R_WORK);
+                Z(Z_ETD4_S2, R_WORK);
+                X(XY_FUSED, R_WORK);
+                Z(Z_ETD4_S3, R_WORK);
+                X(XY_FUSED, R_WORK);
+                Z(Z_ETD4_S4, R_CAND);
+                X(XY_FUSED, R_CAND);
+                break;
+            default:
+                Z(Z_EULER, R_CAND);
+                X(XY_FUSED, R_CAND);
+                break;
+        }
+    } else {
     switch (method) {
         case M_ETD2:
             X(XY_NONLIN, R_STATE, 1);
@@ -276,6 +312,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             X(XY_REDUCE_FULL, R_CAND);
             break;
     }
+    }
     timed(K_DECIDE, [&]() { return Launch<T>::decide(d, ninst, raw ? 1 : 0, s); });
     return r;
 }
@@ -299,8 +336,8 @@ template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* l
     const int ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t fs = al(ns * 16), fp = al(ns * sizeof(T) * 2);
-    // Nu, P x6, A, B (+ Na, Nb), then the split path's Y0, Y1
-    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0);
+    // Nu, P x6, A, B (+ Na, Nb), then the split path's Y0, Y1, then the FP32 form's G slots
+    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0) + (sizeof(T) == 4 ? 4 : 0);
     // FP32 form: the FP64 plain transforms of set/get phi need their own Y0, Y1
     const int naux = (sizeof(T) == 4 && uses_split<double>(p)) ? 2 : 0;
     size_t off = 0;
@@ -363,8 +400,11 @@ template <class T> class Stepper final : public Handle {
                         &h.A, &h.B, &h.Na, &h.Nb};
         const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0);
         for (int i = 0; i < nplain; ++i) *f[i] = base + lay[6] + i * fp;
+        int nextf = nplain;
         if (uses_split<T>(p))
-            for (int i = 0; i < 2; ++i) h.Y[i] = base + lay[6] + (nplain + i) * fp;
+            for (int i = 0; i < 2; ++i) h.Y[i] = base + lay[6] + (nextf++) * fp;
+        if (sizeof(T) == 4)
+            for (int i = 0; i < 4; ++i) h.G[i / 2][i % 2] = base + lay[6] + (nextf++) * fp;
         h.coef = reinterpret_cast<T*>(base + lay[1]);
         h.part_xy = reinterpret_cast<double*>(base + lay[2]);
         h.part_z = reinterpret_cast<double*>(base + lay[3]);
@@ -455,7 +495,8 @@ template <class T> class Stepper final : public Handle {
             CB_CK(fwd3d(src, h.spec[0], h.A, true));
         }
         CB_CK(zpass(Z_INV_STATE, R_STATE));
-        CB_CK(xypass(XY_REDUCE_FULL, R_STATE));
+        // FP32 form: the fused pass also leaves the state's nonlinear partials in its G slot
+        CB_CK(xypass(sizeof(T) == 4 ? XY_FUSED : XY_REDUCE_FULL, R_STATE));
         CB_CK(pull());
         // alpha/beta from t = 0 when beta <= 0 (fluidbase.cpp:143, belastic.cpp:588-591)
         if (!(up.beta > 0.0)) {
@@ -671,7 +712,7 @@ template <class T> class Stepper final : public Handle {
                 hc.done = 0;
                 CB_CK(push());
                 CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
-                CB_CK(xypass(XY_NONLIN, R_STATE));
+                if (sizeof(T) == 8) CB_CK(xypass(XY_NONLIN, R_STATE));  // FP32: the state's G slot holds them
                 CB_CK(zpass(etd ? (p.method == M_ETD2 ? Z_ETD2_S1 : Z_ETD4_S1) : Z_EULER, etd ? R_WORK : R_CAND));
                 if (etd) CB_CK(Launch<T>::nhat_full(d, h.spec[hc.spec_state], dst, ns, st));
                 else CB_CK(inv3d(h.Nu, SM_NONE, dst));

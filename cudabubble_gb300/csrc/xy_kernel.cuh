@@ -13,6 +13,9 @@
 //   XY_NONLIN       u, lap u -> pointwise nonlinearity G and H, forward xy
 //                   transforms, written as the partials A = G^ + beta cx (kx^2+ky^2) H^
 //                   and B = H^ that the z pass turns into the nonlinear spectrum
+//   XY_FUSED        (FP32 form) the sums of XY_REDUCE_FULL and, with lambda = 0,
+//                   the partials of XY_NONLIN, in one pass; the z pass adds the
+//                   penalty terms lambda1, lambda2 f spectrally once the sums exist
 //   XY_INV_PLAIN    partial -> real plane (double out)
 //   XY_FWD_PLAIN    real plane (double in) -> partial
 // The pointwise formulas restate Calc.cu:153-162 (f), :171-180 (g0),
@@ -47,7 +50,51 @@ __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* su
     }
 }
 
-// NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN, 1 otherwise
+// Per-CTA partial sums (slot `slot` of `nslots`) of u, (u^2 - 1)^2, f^2, then
+// the last CTA of the instance finalises the role's scalars; all threads call.
+template <class T, class V>
+__device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Params& p, int slot, int nslots, V* vv,
+                                        double* red, int role, bool full) {
+    double v[3];
+    block_sum<3>(vv, v, red);
+    double* part = I.part_xy;
+    int* last = reinterpret_cast<int*>(red + 128);
+    if (threadIdx.x == 0) {
+        part[4 * slot + 0] = v[0];
+        part[4 * slot + 1] = v[1];
+        part[4 * slot + 2] = v[2];
+        part[4 * slot + 3] = 0.0;
+        __threadfence();
+        const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[role], 1u);
+        *last = done_blocks == (unsigned)(nslots - 1);
+    }
+    __syncthreads();
+    if (*last) {  // the last CTA of this instance finalises, with all its threads
+        __threadfence();
+        double sums[4];
+        block_sum_parts<4>(part, nslots, sums, red);
+        if (threadIdx.x == 0) {
+            finalize_xy(p, ctrl, sums, role, full);
+            ctrl->cnt_xy[role] = 0u;
+        }
+    }
+}
+
+// where a nonlinear pass leaves its two forward-transformed fields: the work
+// pair A, B, or (XY_FUSED of the state / candidate) that role's G slot
+template <class T>
+__device__ __forceinline__ void nl_outputs(const InstT<T>& I, const Ctrl* c, int mode, int role, void*& A, void*& B) {
+    if (mode == XY_FUSED && role != R_WORK) {
+        const int sl = role == R_STATE ? c->ab_state : 1 - c->ab_state;
+        A = I.G[sl][0];
+        B = I.G[sl][1];
+    } else {
+        A = I.A;
+        B = I.B;
+    }
+}
+
+// NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN / XY_FUSED, 1 otherwise
 template <class T, int NX, int NT, int NF>
 __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
     using C = cplx<T>;
@@ -61,7 +108,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     const int z = blockIdx.x;
     const int tid = threadIdx.x;
     if (z >= p.nz) return;
-    const bool stepping = a.mode <= XY_NONLIN;
+    const bool stepping = a.mode <= XY_FUSED;
     if (stepping) {
         if (ctrl->done) return;
         if (a.skip_if_stale && !ctrl->fresh) return;
@@ -109,23 +156,16 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             P0 = reinterpret_cast<const C*>(I.P[set][0]) + (size_t)z * plane;
             P2 = reinterpret_cast<const C*>(I.P[set][1]) + (size_t)z * plane;
         }
-        for (int it = tid; it < NY * M; it += NT) {
+        // store one loaded element (and, in column 0, its Nyquist partner) into the plane
+        auto put = [&](int it, C v, C w, C vN, C wN) {
             const int c = it % M, ky = it / M;
-            const C v = P0[ky * NC + c];
-            C vN = cmk<C>(0, 0);
-            if (c == 0) {
-                vN = P0[ky * NC + M];
-                S[ky * pitch] = cmk<C>(v.x - vN.y, v.y + vN.x);  // col0 + i*colN
-            } else {
-                S[ky * pitch + c] = v;
-            }
+            if (c == 0) S[ky * pitch] = cmk<C>(v.x - vN.y, v.y + vN.x);  // col0 + i*colN
+            else S[ky * pitch + c] = v;
             if (nf == 2) {  // laplacian partial Q = -cx (kx^2 + ky^2) P0 + P2 (Calc.cu:107-124)
                 const int kyf = min(ky, NY - ky);
-                const C w = P2[ky * NC + c];
                 if constexpr (sizeof(T) == 8) {
                     const T kyy = cx * (T)(kyf * kyf);
                     if (c == 0) {
-                        const C wN = P2[ky * NC + M];
                         const T kN = cx * (T)(M * M) + kyy;
                         const C q0 = cmk<C>(w.x - kyy * v.x, w.y - kyy * v.y);
                         const C qN = cmk<C>(wN.x - kN * vN.x, wN.y - kN * vN.y);
@@ -140,12 +180,38 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                         return cmk<C>(ww.x - kcx.mul((T)kk * vv.x), ww.y - kcx.mul((T)kk * vv.y));
                     };
                     if (c == 0) {
-                        const C q0 = q(w, v, kyf * kyf), qN = q(P2[ky * NC + M], vN, M * M + kyf * kyf);
+                        const C q0 = q(w, v, kyf * kyf), qN = q(wN, vN, M * M + kyf * kyf);
                         S[ky * pitch + M] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
                     } else {
                         S[ky * pitch + M + c] = q(w, v, c * c + kyf * kyf);
                     }
                 }
+            }
+        };
+        // loads in batches of LB per thread, all issued before any is used: the
+        // plane load is latency-bound with one load in flight per thread
+        constexpr int LB = 4;
+        constexpr int ITER = (NY * M + NT - 1) / NT;
+        for (int b0 = 0; b0 < ITER; b0 += LB) {
+            C v[LB], w[LB], vN[LB], wN[LB];
+#pragma unroll
+            for (int j = 0; j < LB; ++j) {
+                const int it = tid + (b0 + j) * NT;
+                v[j] = w[j] = vN[j] = wN[j] = cmk<C>(0, 0);
+                if (b0 + j < ITER && it < NY * M) {
+                    const int c = it % M, ky = it / M;
+                    v[j] = __ldg(P0 + ky * NC + c);
+                    if (nf == 2) w[j] = __ldg(P2 + ky * NC + c);
+                    if (c == 0) {
+                        vN[j] = __ldg(P0 + ky * NC + M);
+                        if (nf == 2) wN[j] = __ldg(P2 + ky * NC + M);
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < LB; ++j) {
+                const int it = tid + (b0 + j) * NT;
+                if (b0 + j < ITER && it < NY * M) put(it, v[j], w[j], vN[j], wN[j]);
             }
         }
         __syncthreads();
@@ -211,6 +277,27 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 *pl = h;
             }
             __syncthreads();
+        } else if (a.mode == XY_FUSED) {
+            // sums of the state and its lambda-free partials G'', w in one sweep
+            const bool euler = p.method == M_EULER;
+            Acc<T> au, as, af;
+            for (int it = tid; it < NY * M; it += NT) {
+                const int q = it % M, r = it / M;
+                C* pu = S + r * pitch + q;
+                C* pl = pu + M;
+                const C uu = *pu, ll = *pl;
+                reduce_point<T>(k, true, uu.x, ll.x, au, as, af);
+                reduce_point<T>(k, true, uu.y, ll.y, au, as, af);
+                C g, h;
+                nonlin_point<T>(k, euler, (T)0, (T)0, uu.x, ll.x, g.x, h.x);
+                nonlin_point<T>(k, euler, (T)0, (T)0, uu.y, ll.y, g.y, h.y);
+                *pu = g;
+                *pl = h;
+            }
+            auto pv = au.part();
+            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, true);
+            __syncthreads();
         } else {
             // reductions (XY_REDUCE_FULL / XY_REDUCE_S)
             const bool full = a.mode == XY_REDUCE_FULL;
@@ -224,35 +311,13 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             }
             auto pv = au.part();
             decltype(pv) vv[3] = {pv, as.part(), af.part()};
-            double v[3];
-            block_sum<3>(vv, v, red);
-            double* part = I.part_xy;
-            int* last = reinterpret_cast<int*>(red + 128);
-            if (tid == 0) {
-                part[4 * z + 0] = v[0];
-                part[4 * z + 1] = v[1];
-                part[4 * z + 2] = v[2];
-                part[4 * z + 3] = 0.0;
-                __threadfence();
-                const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[a.role], 1u);
-                *last = done_blocks == (unsigned)(p.nz - 1);
-            }
-            __syncthreads();
-            if (*last) {  // the last CTA of this instance finalises, with all its threads
-                __threadfence();
-                double sums[4];
-                block_sum_parts<4>(part, p.nz, sums, red);
-                if (tid == 0) {
-                    finalize_xy(p, ctrl, sums, a.role, full);
-                    ctrl->cnt_xy[a.role] = 0u;
-                }
-            }
+            xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, full);
             return;
         }
     }
 
     // ---- forward xy: x R2C (transposed in, natural out) then y (transposed in, natural out)
-    constexpr int nfo = NF;  // XY_NONLIN (2 fields) or XY_FWD_PLAIN (1)
+    constexpr int nfo = NF;  // XY_NONLIN / XY_FUSED (2 fields) or XY_FWD_PLAIN (1)
     const PairRows<NY, pitch, M> rows;
     fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl);
     __syncthreads();
@@ -285,9 +350,11 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
     C* outA;
     C* outB = nullptr;
-    if (a.mode == XY_NONLIN) {
-        outA = reinterpret_cast<C*>(I.A) + (size_t)z * plane;
-        outB = reinterpret_cast<C*>(I.B) + (size_t)z * plane;
+    if (a.mode == XY_NONLIN || a.mode == XY_FUSED) {
+        void *oa, *ob;
+        nl_outputs<T>(I, ctrl, a.mode, a.role, oa, ob);
+        outA = reinterpret_cast<C*>(oa) + (size_t)z * plane;
+        outB = reinterpret_cast<C*>(ob) + (size_t)z * plane;
     } else {
         outA = reinterpret_cast<C*>(a.cout) + (size_t)z * plane;
     }

@@ -36,7 +36,7 @@ template <> struct State<double> {
     double2 v;
     __device__ __forceinline__ static State load(const void* p, size_t g) {
         State s;
-        s.v = reinterpret_cast<const double2*>(p)[g];
+        s.v = __ldg(reinterpret_cast<const double2*>(p) + g);
         return s;
     }
     __device__ __forceinline__ static State from(double2 w) { State s; s.v = w; return s; }
@@ -66,7 +66,7 @@ __device__ __forceinline__ void df_add(float& h, float& l, float d) {
 template <> struct State<float> {
     float2 hi, lo;
     __device__ __forceinline__ static State load(const void* p, size_t g) {
-        const float4 q = reinterpret_cast<const float4*>(p)[g];
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p) + g);
         State s;
         s.hi = make_float2(q.x, q.y);
         s.lo = make_float2(q.z, q.w);
@@ -110,8 +110,18 @@ template <> struct State<float> {
     }
 };
 
-template <class T, int NZ, int TX, int NT>
+// Mode groups: each z_kernel instance compiles only its group's stage code, so
+// the ETD-RK2 instance does not carry the registers of the ETD-RK4 combine.
+enum ZGroup { ZG_ETD2 = 0, ZG_ETD4 = 1, ZG_EULER = 2, ZG_PLAIN = 3 };
+__host__ __device__ constexpr int zgroup_of(int mode) {
+    return (mode == Z_ETD2_S1 || mode == Z_ETD2_S2) ? ZG_ETD2
+         : (mode >= Z_ETD4_S1 && mode <= Z_ETD4_S4) ? ZG_ETD4
+         : mode == Z_EULER ? ZG_EULER : ZG_PLAIN;
+}
+
+template <class T, int NZ, int TX, int NT, int MG>
 __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+    constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const InstT<T>& I = insts[blockIdx.y];
@@ -138,18 +148,43 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
     const bool need_fwd = (a.mode <= Z_EULER && !reuse) || a.mode == Z_FWD_PLAIN;
 
     if (need_fwd) {
-        const C* gA = reinterpret_cast<const C*>(a.mode == Z_FWD_PLAIN ? a.cin : I.A);
-        const C* gB = reinterpret_cast<const C*>(I.B);
-        const bool two = a.mode != Z_FWD_PLAIN;
-        for (int it = tid; it < NZ * TX; it += NT) {
-            const int c = it % TX, zz = it / TX, m = m0 + c;
-            C va = cmk<C>(0, 0), vb = cmk<C>(0, 0);
-            if (m < Mc) {
-                va = gA[(size_t)zz * Mc + m];
-                if (two) vb = gB[(size_t)zz * Mc + m];
+        // stage 1 of the FP32 form reads the state's fused-pass outputs (G slot)
+        const void* srcA = I.A;
+        const void* srcB = I.B;
+        if constexpr (sizeof(T) == 4) {
+            if (stage1) {
+                srcA = I.G[ctrl->ab_state][0];
+                srcB = I.G[ctrl->ab_state][1];
             }
-            S[zz * W + c] = va;
-            S[zz * W + TX + c] = vb;
+        }
+        const C* gA = reinterpret_cast<const C*>(a.mode == Z_FWD_PLAIN ? a.cin : srcA);
+        const C* gB = reinterpret_cast<const C*>(srcB);
+        const bool two = a.mode != Z_FWD_PLAIN;
+        // batches of LB loads per thread in flight before the shared-memory stores
+        constexpr int LB = 4;
+        constexpr int ITER = (NZ * TX + NT - 1) / NT;
+        for (int b0 = 0; b0 < ITER; b0 += LB) {
+            C va[LB], vb[LB];
+#pragma unroll
+            for (int j = 0; j < LB; ++j) {
+                const int it = tid + (b0 + j) * NT;
+                va[j] = vb[j] = cmk<C>(0, 0);
+                const int m = m0 + it % TX;
+                if (b0 + j < ITER && it < NZ * TX && m < Mc) {
+                    const size_t gi = (size_t)(it / TX) * Mc + m;
+                    va[j] = __ldg(gA + gi);
+                    if (two) vb[j] = __ldg(gB + gi);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < LB; ++j) {
+                const int it = tid + (b0 + j) * NT;
+                if (b0 + j < ITER && it < NZ * TX) {
+                    const int c = it % TX, zz = it / TX;
+                    S[zz * W + c] = va[j];
+                    S[zz * W + TX + c] = vb[j];
+                }
+            }
         }
         __syncthreads();
         if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw, twl);
@@ -185,10 +220,16 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
     C* Nb = reinterpret_cast<C*>(I.Nb);
     void* ah = I.ahat;
     const T* coef = I.coef + (size_t)ctrl->tab_cur * (size_t)(p.kmax + 1) * 8;
-    T* bc = reinterpret_cast<T*>(red);  // dt * ga, formed once per CTA
-    if (tid == 0) bc[0] = (T)(ctrl->dt * p.ga);
+    T* bc = reinterpret_cast<T*>(red);  // dt * ga and (FP32 form) the lambda terms, once per CTA
+    if (tid == 0) {
+        bc[0] = (T)(ctrl->dt * p.ga);
+        if constexpr (sizeof(T) == 4) {  // of the state the fused pass evaluated
+            if (a.mode <= Z_EULER) nonlin_lambdas<T>(p, ctrl, stage1 ? R_STATE : R_WORK, bc + 1);
+        }
+    }
     __syncthreads();
     const T dtga = bc[0];
+    const T g_c = sizeof(T) == 4 ? bc[1] : (T)0, g_f = sizeof(T) == 4 ? bc[2] : (T)0;
     const bool ref4 = p.etd4_ref != 0;
     Acc<T> ag, ag2, al;
     static_assert(NT % TX == 0, "one column per thread");
@@ -208,7 +249,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
         const int kz = tidx<NZ>(r);
         const int kzf = min(kz, NZ - kz);
         const size_t g = (size_t)kz * Mc + m;
-        C nh = cmk<C>(0, 0);
+        C nh = cmk<C>(0, 0), wn = cmk<C>(0, 0);
         if (need_fwd) {
             const C va = S[r * W + c], vb = S[r * W + TX + c];
             if constexpr (sizeof(T) == 8) {
@@ -217,8 +258,29 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
             } else {  // beta cx and 1/N folded hi + lo: no systematic gain on N-hat
                 const T kk = (T)(kzf * kzf);
                 nh = cmk<C>(k.k_invN.mul(va.x + k.k_bnl.mul(kk * vb.x)), k.k_invN.mul(va.y + k.k_bnl.mul(kk * vb.y)));
+                wn = cmk<C>(k.k_invN.mul(vb.x), k.k_invN.mul(vb.y));
             }
         }
+        // FP32 form: the penalty terms of the fused pass's state x,
+        //   + lambda-constant at k = 0 and + g_f f-hat(x), f-hat = eps cx |k|^2 x-hat + w-hat / eps (ETD)
+        //   or the transformed f itself (Euler)
+        const int kk_full = kxy + kzf * kzf;
+        auto add_lam = [&](C& v, C xh) {
+            if constexpr (sizeof(T) == 4) {
+                C fh;
+                if (a.mode == Z_EULER) {
+                    fh = wn;
+                } else {
+                    const T kf = (T)kk_full;
+                    fh = cmk<C>(k.k_ieps.mul(wn.x) + k.k_eps.mul(k.k_cx.mul(kf * xh.x)),
+                                k.k_ieps.mul(wn.y) + k.k_eps.mul(k.k_cx.mul(kf * xh.y)));
+                }
+                v.x = fmaf(g_f, fh.x, v.x);
+                v.y = fmaf(g_f, fh.y, v.y);
+                if (m == 0 && kz == 0) v.x += g_c;
+            }
+            (void)xh;
+        };
         const T* cf = coef + 8 * (kxy + kzf * kzf);
         State<T> us;           // the new stage / state spectrum
         bool have_state = true;
@@ -230,14 +292,23 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
             switch (a.mode) {
                 case Z_ETD2_S1:
                 case Z_ETD4_S1: {  // a = phi (+) (em' phi + c1 N'_u)
-                    if (reuse) nh = Nu[g]; else Nu[g] = nh;
-                    us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
+                    if constexpr (!(g2 || g4)) break;
+                    const State<T> sp = State<T>::load(phat, g);
+                    if (reuse) {
+                        nh = Nu[g];
+                    } else {
+                        add_lam(nh, sp.work());
+                        Nu[g] = nh;
+                    }
+                    us = sp.axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                     us.store(ah, g);
                     break;
                 }
                 case Z_ETD2_S2: {  // phi' = a (+) (c2 (N'_a - N'_u) + c2 c_lin d_a)
+                    if constexpr (!g2) break;
                     const C nu = Nu[g];
                     const State<T> sa = State<T>::load(ah, g);
+                    add_lam(nh, sa.work());
                     const float2 da = sa.diff(State<T>::load(phat, g));
                     us = sa.add(cmk<C>(fmaf(cf[3], da.x, cf[2] * (nh.x - nu.x)), fmaf(cf[3], da.y, cf[2] * (nh.y - nu.y))));
                     us.store(cand, g);
@@ -246,6 +317,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                 case Z_ETD4_S2:
                 case Z_ETD4_S3:
                 case Z_ETD4_S4: {
+                    if constexpr (!g4) break;
                     const State<T> sp = State<T>::load(phat, g), sa = State<T>::load(ah, g);
                     const float2 da = sa.diff(sp);
                     const T emh = cf[0], ch = cf[1], chcl = cf[6];
@@ -254,6 +326,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                         return cmk<C>(fmaf(chcl, da.x, ch * na.x), fmaf(chcl, da.y, ch * na.y));
                     };
                     if (a.mode == Z_ETD4_S2) {
+                        add_lam(nh, sa.work());
                         Na[g] = nh;
                         us = sp.axpy(emh, inc_b(nh));
                         break;
@@ -261,12 +334,14 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                     const C na = Na[g], nu = Nu[g];
                     const C ib = inc_b(na);
                     const float2 db = make_float2(fmaf(emh, sp.hi.x, ib.x), fmaf(emh, sp.hi.y, ib.y));
+                    const C spw = sp.work();
                     // increment of c = a (+) (em'_h a + c_h (2 N'_b - N'_u) + c_h c_lin (2 d_b - d_a))
                     auto inc_c = [&](C nb) {
                         return cmk<C>(fmaf(chcl, (T)2 * db.x - da.x, ch * ((T)2 * nb.x - nu.x)),
                                       fmaf(chcl, (T)2 * db.y - da.y, ch * ((T)2 * nb.y - nu.y)));
                     };
                     if (a.mode == Z_ETD4_S3) {
+                        add_lam(nh, cmk<C>(spw.x + db.x, spw.y + db.y));  // b = phi + d_b
                         Nb[g] = nh;
                         us = sa.axpy(emh, inc_c(nh));
                         break;
@@ -276,6 +351,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                     const C nb = Nb[g];
                     const C ic = inc_c(nb);
                     const float2 dc = make_float2(da.x + fmaf(emh, sa.hi.x, ic.x), da.y + fmaf(emh, sa.hi.y, ic.y));
+                    add_lam(nh, cmk<C>(spw.x + dc.x, spw.y + dc.y));  // c = phi + d_c
                     const T f1 = cf[3], f2 = cf[4], f3 = cf[5], cl = cf[7];
                     const C n1 = ref4 ? na : nu;
                     const float2 d1 = ref4 ? da : make_float2(0.f, 0.f);
@@ -291,29 +367,34 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
         }
         switch (sizeof(T) == 4 && a.mode <= Z_ETD4_S4 ? -1 : a.mode) {
             case Z_ETD2_S1: {  // a = e phi + c1 N_u (Calc.cu:453-455)
+                if constexpr (!g2) break;
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
                 us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                 us.store(ah, g);
                 break;
             }
             case Z_ETD2_S2: {  // phi' = a + c2 (N_a - N_u) (Calc.cu:476-477)
+                if constexpr (!g2) break;
                 const C nu = Nu[g];
                 us = State<T>::load(ah, g).add(cmk<C>(cf[2] * (nh.x - nu.x), cf[2] * (nh.y - nu.y)));
                 us.store(cand, g);
                 break;
             }
             case Z_ETD4_S1: {  // a = e_h phi + c_h N_u (Calc.cu:495-497)
+                if constexpr (!g4) break;
                 if (reuse) nh = Nu[g]; else Nu[g] = nh;
                 us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                 us.store(ah, g);
                 break;
             }
             case Z_ETD4_S2: {  // b = e_h phi + c_h N_a (Calc.cu:516-518)
+                if constexpr (!g4) break;
                 Na[g] = nh;
                 us = State<T>::load(phat, g).axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                 break;
             }
             case Z_ETD4_S3: {  // c = e_h a + c_h (2 N_b - N_u) (Calc.cu:537-538)
+                if constexpr (!g4) break;
                 Nb[g] = nh;
                 const C nu = Nu[g];
                 us = State<T>::load(ah, g).axpy(
@@ -322,6 +403,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
             }
             case Z_ETD4_S4: {  // e2 phi + f1 N1 + f2 (N_a + N_b) + f3 N_c (Calc.cu:556-567)
                 // N1 = N_a in the reference (belastic.cpp:550), N_u in Cox-Matthews
+                if constexpr (!g4) break;
                 const T f1 = cf[3], f2 = cf[4], f3 = cf[5];
                 const C na = Na[g], n1 = ref4 ? na : Nu[g], nb = Nb[g];
                 const C inc = cmk<C>(f1 * n1.x + f2 * (na.x + nb.x) + f3 * nh.x,
@@ -332,17 +414,25 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
             }
             case -1: break;  // FP32 ETD stages, above
             case Z_EULER: {  // phi' = phi - dt ga R (Calc.cu:393-402)
-                if (reuse) nh = Nu[g]; else Nu[g] = nh;
+                if constexpr (!ge) break;
+                if (reuse) {
+                    nh = Nu[g];
+                } else {
+                    add_lam(nh, cmk<C>(0, 0));
+                    Nu[g] = nh;
+                }
                 us = State<T>::load(phat, g).add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
                 us.store(cand, g);
                 al.add(wxy * (nh.x * nh.x + nh.y * nh.y));
                 break;
             }
             case Z_INV_STATE: {
+                if constexpr (!gp) break;
                 us = State<T>::load(spec_of(I, ctrl, a.role), g);
                 break;
             }
             default: {  // Z_INV_PLAIN with an optional spectral multiplier
+                if constexpr (!gp) break;
                 have_state = false;
                 const C v = (a.state_io & IO_CIN_STATE) ? State<T>::load(a.cin, g).work()
                                                         : reinterpret_cast<const C*>(a.cin)[g];

@@ -161,9 +161,9 @@ long long cb_handle_bytes(cb_handle* h);
  * the timed pairs) so every attempt starts with a cold L2.  device_ms is the
  * summed attempt time.
  * cb_profile_kernels: nattempts loop attempts launched kernel by kernel with
- * an event pair around each launch; ms[k] / counts[k] per kernel kind
- * k = 0 xy nonlinear pass, 1 xy reduce (S only), 2 xy reduce (full),
- * 3 z pass, 4 decide + coefficient table. */
+ * an event pair around each launch; ms[k] / counts[k] (6 entries each) per
+ * kernel kind k = 0 xy nonlinear pass, 1 xy reduce (S only), 2 xy reduce
+ * (full), 3 z pass, 4 decide + coefficient table, 5 xy fused pass (FP32). */
 int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts);
 int cb_profile_kernels(cb_handle* h, int nattempts, long long flush_bytes, double* ms, int* counts);
 
