@@ -69,18 +69,49 @@ __device__ __forceinline__ void nonlin_point(const PC<T>& k, bool euler, T g_c, 
     }
 }
 
-// sums of one real point: u, (u^2 - 1)^2 and (full) f^2 (phasefield.cpp:283-325)
+// sums of one real point: (u^2 - 1)^2 and (full) f^2 (phasefield.cpp:293-325;
+// the volume comes from the k = 0 mode in the z pass)
 template <class T>
-__device__ __forceinline__ void reduce_point(const PC<T>& k, bool full, T u, T lap, Acc<T>& au, Acc<T>& as,
-                                             Acc<T>& af) {
+__device__ __forceinline__ void reduce_point(const PC<T>& k, bool full, T u, T lap, Acc<T>& as, Acc<T>& af) {
     const T u2m = u * u - (T)1;
-    au.add(u);
     as.add(u2m * u2m);
     if (full) {
         T f;
         if constexpr (sizeof(T) == 8) f = -lap * k.eps + u2m * u * k.ieps;
         else f = k.k_ieps.mul(u2m * u) - k.k_eps.mul(lap);
         af.add(f * f);
+    }
+}
+
+// XY_FUSED point (FP32 form): the sums of reduce_point and the lambda-free
+// partials of nonlin_point (g_c = g_f = 0) from one evaluation of f
+template <class T>
+__device__ __forceinline__ void fused_point(const PC<T>& k, bool euler, T u, T lap, Acc<T>& as, Acc<T>& af, T& g,
+                                            T& h) {
+    const T D = (T)1.5;
+    const T u2 = u * u;
+    const T u2m = u2 - (T)1;
+    const T w = u2m * u;
+    T f;
+    if constexpr (sizeof(T) == 8) f = -lap * k.eps + w * k.ieps;
+    else f = k.k_ieps.mul(w) - k.k_eps.mul(lap);
+    as.add(u2m * u2m);
+    af.add(f * f);
+    if constexpr (sizeof(T) == 8) {  // not used by the FP64 form; kept total
+        const T t = u * (u2 - (T)3);
+        if (euler) {
+            g = k.eta * ((T)3 * u2 - (T)1) * f * k.ieps2;
+            h = f;
+        } else {
+            g = -k.eta * (D * t * k.ieps3 + ((T)3 * u2 - D - (T)1) * k.ieps2 * f);
+            h = t;
+        }
+    } else if (euler) {
+        g = k.k_K2.mul(((T)3 * u2 - (T)1) * f);
+        h = f;
+    } else {
+        g = -(k.k_K3.mul(w) + k.k_K2.mul(((T)3 * u2 - D - (T)1) * f));
+        h = w;
     }
 }
 

@@ -239,36 +239,34 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
             __syncthreads();
         } else if (a.mode == XY_FUSED) {
             const bool euler = p.method == M_EULER;
-            Acc<T> au, as, af;
+            Acc<T> as, af;
             for (int it = tid; it < RPC * M; it += NT) {
                 const int q = it % M, j = it / M;
                 C* pu = S + j * LP + q;
                 C* pl = S + (RPC + j) * LP + q;
                 const C uu = *pu, ll = *pl;
-                reduce_point<T>(k, true, uu.x, ll.x, au, as, af);
-                reduce_point<T>(k, true, uu.y, ll.y, au, as, af);
                 C g, h;
-                nonlin_point<T>(k, euler, (T)0, (T)0, uu.x, ll.x, g.x, h.x);
-                nonlin_point<T>(k, euler, (T)0, (T)0, uu.y, ll.y, g.y, h.y);
+                fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
+                fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
                 *pu = g;
                 *pl = h;
             }
-            auto pv = au.part();
-            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            auto pv = as.part();
+            decltype(pv) vv[2] = {pv, af.part()};
             xy_sums_finalize<T>(I, ctrl, p, rb, nblk, vv, red, a.role, true);
             __syncthreads();
         } else {
             const bool full = a.mode == XY_REDUCE_FULL;
-            Acc<T> au, as, af;
+            Acc<T> as, af;
             for (int it = tid; it < RPC * M; it += NT) {
                 const int q = it % M, j = it / M;
                 const C uu = S[j * LP + q];
                 const C ll = full ? S[(RPC + j) * LP + q] : cmk<C>(0, 0);
-                reduce_point<T>(k, full, uu.x, ll.x, au, as, af);
-                reduce_point<T>(k, full, uu.y, ll.y, au, as, af);
+                reduce_point<T>(k, full, uu.x, ll.x, as, af);
+                reduce_point<T>(k, full, uu.y, ll.y, as, af);
             }
-            auto pv = au.part();
-            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            auto pv = as.part();
+            decltype(pv) vv[2] = {pv, af.part()};
             xy_sums_finalize<T>(I, ctrl, p, rb, nblk, vv, red, a.role, full);
             return;
         }

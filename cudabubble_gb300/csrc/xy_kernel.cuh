@@ -50,19 +50,19 @@ __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* su
     }
 }
 
-// Per-CTA partial sums (slot `slot` of `nslots`) of u, (u^2 - 1)^2, f^2, then
+// Per-CTA partial sums (slot `slot` of `nslots`) of (u^2 - 1)^2, f^2, then
 // the last CTA of the instance finalises the role's scalars; all threads call.
 template <class T, class V>
 __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Params& p, int slot, int nslots, V* vv,
                                         double* red, int role, bool full) {
-    double v[3];
-    block_sum<3>(vv, v, red);
+    double v[2];
+    block_sum<2>(vv, v, red);
     double* part = I.part_xy;
     int* last = reinterpret_cast<int*>(red + 128);
     if (threadIdx.x == 0) {
-        part[4 * slot + 0] = v[0];
-        part[4 * slot + 1] = v[1];
-        part[4 * slot + 2] = v[2];
+        part[4 * slot + 0] = 0.0;
+        part[4 * slot + 1] = v[0];
+        part[4 * slot + 2] = v[1];
         part[4 * slot + 3] = 0.0;
         __threadfence();
         const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[role], 1u);
@@ -280,37 +280,35 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         } else if (a.mode == XY_FUSED) {
             // sums of the state and its lambda-free partials G'', w in one sweep
             const bool euler = p.method == M_EULER;
-            Acc<T> au, as, af;
+            Acc<T> as, af;
             for (int it = tid; it < NY * M; it += NT) {
                 const int q = it % M, r = it / M;
                 C* pu = S + r * pitch + q;
                 C* pl = pu + M;
                 const C uu = *pu, ll = *pl;
-                reduce_point<T>(k, true, uu.x, ll.x, au, as, af);
-                reduce_point<T>(k, true, uu.y, ll.y, au, as, af);
                 C g, h;
-                nonlin_point<T>(k, euler, (T)0, (T)0, uu.x, ll.x, g.x, h.x);
-                nonlin_point<T>(k, euler, (T)0, (T)0, uu.y, ll.y, g.y, h.y);
+                fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
+                fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
                 *pu = g;
                 *pl = h;
             }
-            auto pv = au.part();
-            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            auto pv = as.part();
+            decltype(pv) vv[2] = {pv, af.part()};
             xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, true);
             __syncthreads();
         } else {
             // reductions (XY_REDUCE_FULL / XY_REDUCE_S)
             const bool full = a.mode == XY_REDUCE_FULL;
-            Acc<T> au, as, af;
+            Acc<T> as, af;
             for (int it = tid; it < NY * M; it += NT) {
                 const int q = it % M, r = it / M;
                 const C uu = S[r * pitch + q];
                 const C ll = full ? S[r * pitch + M + q] : cmk<C>(0, 0);
-                reduce_point<T>(k, full, uu.x, ll.x, au, as, af);
-                reduce_point<T>(k, full, uu.y, ll.y, au, as, af);
+                reduce_point<T>(k, full, uu.x, ll.x, as, af);
+                reduce_point<T>(k, full, uu.y, ll.y, as, af);
             }
-            auto pv = au.part();
-            decltype(pv) vv[3] = {pv, as.part(), af.part()};
+            auto pv = as.part();
+            decltype(pv) vv[2] = {pv, af.part()};
             xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, full);
             return;
         }
