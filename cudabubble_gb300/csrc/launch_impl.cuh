@@ -6,6 +6,7 @@
 #include "launch.h"
 #include "misc_kernels.cuh"
 #include "split_kernels.cuh"
+#include "xy_cluster.cuh"
 #include "xy_kernel.cuh"
 #include "z_kernel.cuh"
 
@@ -30,6 +31,28 @@ template <class T, int NX> struct XYCfg {
     static constexpr bool ok1 = xy_smem_bytes<T, NX>(1) <= kMaxSmem;  // plain transforms (one field)
 };
 
+// FP32 fused pass on two-CTA clusters from 64^2 planes (a build-time knob)
+#ifndef CB_XY_CLUSTER
+#define CB_XY_CLUSTER 1
+#endif
+template <class T, int NX> constexpr bool xyc_ok() {
+    return CB_XY_CLUSTER && sizeof(T) == 4 && NX >= 64 && NX % 4 == 0 && xyc_smem_bytes<T, NX>() <= 227 * 1024;
+}
+template <class T, int NX>
+static cudaError_t xyc_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    constexpr int NT = NX >= 96 ? 512 : 256;
+    constexpr size_t sm = xyc_smem_bytes<T, NX>();
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e =
+            cudaFuncSetAttribute(xyc_fused_kernel<T, NX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    xyc_fused_kernel<T, NX, NT><<<dim3(2 * nzmax, ninst), NT, sm, s>>>(d, a);
+    return cudaGetLastError();
+}
+
 template <class T, int NX, int NF, int NT>
 static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
     static bool attr = false;
@@ -46,6 +69,9 @@ static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArg
 template <class T, int NX>
 static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
     const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED;
+    if constexpr (xyc_ok<T, NX>()) {
+        if (a.mode == XY_FUSED) return xyc_go<T, NX>(d, ninst, nzmax, a, s);
+    }
     if constexpr (XYCfg<T, NX>::ok) {
         if (a.mode == XY_NONLIN || a.mode == XY_FUSED) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN>(d, ninst, nzmax, a, s);
         if (two) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT>(d, ninst, nzmax, a, s);

@@ -326,7 +326,7 @@ template <class T> inline bool uses_split(const Params& p) {
 }
 // per-plane or per-row-block partial sums of the xy reductions
 template <class T> inline size_t xy_part_slots(const Params& p) {
-    size_t n = (size_t)p.nz;
+    size_t n = 2 * (size_t)p.nz;  // two per plane for the two-CTA fused pass
     if (uses_split<T>(p)) n = std::max(n, (size_t)p.nz * p.ny / Launch<T>::xy_rows_per_cta(p.nx));
     return n;
 }
