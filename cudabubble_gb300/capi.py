@@ -20,6 +20,8 @@ CB_EULER, CB_ETD2, CB_ETD4 = 0, 1, 2
 CB_FP64, CB_FP32 = 0, 1
 (CB_FIELD_PHI, CB_FIELD_FD, CB_FIELD_LAP, CB_FIELD_F, CB_FIELD_G0, CB_FIELD_NLD, CB_FIELD_DX, CB_FIELD_DY,
  CB_FIELD_DZ, CB_FIELD_S, CB_FIELD_NLD_HAT, CB_FIELD_RHS) = range(12)
+(CB_RUNNING, CB_DONE_TARGET, CB_DONE_DT_UNDERFLOW, CB_DONE_SMALL_ENERGY, CB_DONE_NONFINITE, CB_DONE_CONVERGED,
+ CB_DONE_TMAX) = range(7)
 STATUS_NAMES = {0: "running", 1: "target", 2: "dt_underflow", 3: "small_energy", 4: "nonfinite", 5: "converged",
                 6: "tmax"}
 ERROR_NAMES = {CB_EINVAL: "CB_EINVAL", CB_ENOMEM: "CB_ENOMEM", CB_ECUDA: "CB_ECUDA", CB_ENONFINITE: "CB_ENONFINITE",
@@ -88,6 +90,7 @@ SIGNATURES = {
     "cb_run": (C.c_int, [C.c_void_p, C.c_int, _P(cb_run_stats)]),
     "cb_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "cb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
+    "cb_set_loop_state": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
     "cb_synchronize": (C.c_int, [C.c_void_p]),
     "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
@@ -217,6 +220,10 @@ class Stepper:
 
     def set_dt(self, dt: float):
         check(lib().cb_set_dt(self.h, dt))
+
+    def set_loop_state(self, t: float, dt: float, alpha: float, beta: float):
+        """Resume a run: accepted time, dt and volume / area targets (after set_phi)."""
+        check(lib().cb_set_loop_state(self.h, t, dt, alpha, beta))
 
     def run_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
         ms = C.c_double(0.0)

@@ -144,6 +144,10 @@ int cb_field(cb_handle* h, int which, double* out, int on_device) {
     return h->impl->field(which, out, on_device != 0);
 }
 int cb_set_dt(cb_handle* h, double dt) { CB_H(h); return h->impl->set_dt(dt); }
+int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double beta) {
+    CB_H(h);
+    return h->impl->set_loop_state(t, dt, alpha, beta);
+}
 int cb_synchronize(cb_handle* h) { CB_H(h); return h->impl->sync(); }
 int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts) {
     CB_H(h);

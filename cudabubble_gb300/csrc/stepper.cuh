@@ -203,6 +203,7 @@ struct Handle {
     virtual int run(int nsteps, cb_run_stats* st) = 0;
     virtual int field(int which, double* out, bool dev) = 0;
     virtual int set_dt(double dt) = 0;
+    virtual int set_loop_state(double t, double dt, double alpha, double beta) = 0;
     virtual int sync() = 0;
     virtual long long bytes() const = 0;
     virtual int run_timed(int nsteps, long long flush_bytes, double* ms, int* attempts) = 0;
@@ -562,6 +563,27 @@ template <class T> class Stepper final : public Handle {
         if (!(dt > 0)) return fail(CB_EINVAL, "dt must be positive");
         CB_CK(pull());
         hc.dt = dt;
+        CB_CK(push());
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    // resume a run: accepted time, dt and the volume / area targets of the
+    // reference's .info file (fluidbase.cpp:2797-2826), the state set before
+    int set_loop_state(double t, double dt, double alpha, double beta) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        if (!(dt > 0)) return fail(CB_EINVAL, "dt must be positive");
+        CB_CK(pull());
+        hc.t = t;
+        hc.dt = dt;
+        hc.alpha = hc.alpha0 = alpha;
+        hc.beta = hc.beta0 = beta;
+        Scal& s = hc.sc[R_STATE];
+        const double ve = s.V - alpha, se = s.S - beta;
+        s.E = p.eta * s.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
+        hc.E_state = hc.E_init = s.E;
+        hc.fresh = 1;
         CB_CK(push());
         CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
         CB_CK(cudaStreamSynchronize(st));

@@ -151,6 +151,10 @@ int cb_run(cb_handle* h, int nsteps, cb_run_stats* st);
 int cb_field(cb_handle* h, int which, double* out, int on_device);
 /* set the time step (and drop the cached coefficient table) */
 int cb_set_dt(cb_handle* h, double dt);
+/* resume: accepted time, dt and the volume / area targets alpha, beta of a
+ * reference run (the .info file of fluidbase::load_info, fluidbase.cpp:2797-2826);
+ * call after cb_set_phi, which otherwise takes alpha, beta from the new state */
+int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double beta);
 int cb_synchronize(cb_handle* h);
 /* HBM bytes held by the handle's stepping state */
 long long cb_handle_bytes(cb_handle* h);
