@@ -44,6 +44,11 @@ class Belastic:
         self.st.euler_step()
 
     # ---- loops (belastic.cpp:286-470 / :554-786)
+    def shape_adjust(self, max_steps: int = 0) -> dict:
+        """Unconstrained pre-relaxation (belastic.cpp:174-284); both loops call it
+        first when the run starts at t = 0 with a nonzero shape flag."""
+        return self.st.shape_adjust(max_steps)
+
     def run_static(self, nsteps: int) -> dict:
         assert self.params.method == CB_EULER
         return self.st.run(nsteps)

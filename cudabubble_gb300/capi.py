@@ -52,6 +52,11 @@ class cb_run_stats(C.Structure):
                 ("device_ms", C.c_double)]
 
 
+class cb_adjust_stats(C.Structure):
+    _fields_ = [("steps", C.c_int), ("attempts", C.c_int), ("status", C.c_int), ("graph_launches", C.c_int),
+                ("t", C.c_double), ("E_start", C.c_double), ("E_end", C.c_double), ("device_ms", C.c_double)]
+
+
 class cb_request(C.Structure):
     _fields_ = [("params", cb_params), ("axes", C.c_double * 3), ("centre", C.c_double * 3),
                 ("axes2", C.c_double * 3), ("centre2", C.c_double * 3), ("arrival_s", C.c_double),
@@ -91,6 +96,7 @@ SIGNATURES = {
     "cb_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "cb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
     "cb_set_loop_state": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "cb_shape_adjust": (C.c_int, [C.c_void_p, C.c_int, _P(cb_adjust_stats)]),
     "cb_synchronize": (C.c_int, [C.c_void_p]),
     "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
@@ -224,6 +230,12 @@ class Stepper:
     def set_loop_state(self, t: float, dt: float, alpha: float, beta: float):
         """Resume a run: accepted time, dt and volume / area targets (after set_phi)."""
         check(lib().cb_set_loop_state(self.h, t, dt, alpha, beta))
+
+    def shape_adjust(self, max_steps: int = 0) -> dict:
+        """belastic::shape_adjust (belastic.cpp:174-284) on the current state."""
+        st = cb_adjust_stats()
+        check(lib().cb_shape_adjust(self.h, max_steps, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in cb_adjust_stats._fields_}
 
     def run_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
         ms = C.c_double(0.0)

@@ -46,6 +46,7 @@ struct Ctrl {
     double E_state;   // energy of the accepted state
     double E_init;    // energy at the start of the run (fixed-dt exit test, belastic.cpp:617,727)
     double E_last_attempt;
+    double sa_eng;    // shape adjustment: energy at its last convergence check
     int steps;        // accepted steps
     int attempts;
     int rejects;
@@ -79,6 +80,7 @@ struct Params {
     int kmax;           // largest folded |k|^2 index
     int grow_every;     // grow dt every this many accepted steps
     int split;          // 1: split plane passes for every xy mode
+    int sched;          // SCHED_LOOP: the time loops; SCHED_SHAPE: the shape_adjust rules
     double eps, eta, ga, M1, M2;
     double cx;          // (2 pi / L)^2
     double L3;          // box volume
@@ -119,6 +121,9 @@ template <> struct PC<double> {
 };
 
 // exit reasons kept in Ctrl::status (mirrors the public CB_* codes)
+// accept / reject and dt rules of an attempt
+enum { SCHED_LOOP = 0, SCHED_SHAPE = 1 };
+
 enum { ST_RUNNING = 0, ST_TARGET = 1, ST_DT_UNDERFLOW = 2, ST_SMALL_ENERGY = 3, ST_NONFINITE = 4, ST_CONVERGED = 5,
        ST_TMAX = 6 };
 

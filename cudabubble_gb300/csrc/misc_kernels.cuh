@@ -45,6 +45,31 @@ __global__ void prologue_kernel(const InstT<T>* __restrict__ insts, int n, int r
     Ctrl* c = I.ctrl;
     const Params& p = I.p;
     if (c->done) return;
+    if (p.sched == SCHED_SHAPE) {
+        // loop head of belastic::shape_adjust (belastic.cpp:204-233), run once per
+        // accepted step: advance tcur (c->t) by dt and count the step (the
+        // reference's counter starts at 1 and is raised before the tests); test
+        // convergence when dt > 1e-4 or int(tcur/dt) is a multiple of int(1e-4/dt);
+        // double dt every tenth count.  The quotients are truncated in 64 bits:
+        // the reference's int conversion has no defined result beyond 2^31.
+        if (c->grow_pending) {
+            c->grow_pending = 0;
+            c->t += c->dt;
+            const int count = c->steps + 2;
+            if (c->dt > 1e-4 || ((long long)(c->t / c->dt)) % ((long long)(1e-4 / c->dt)) == 0) {
+                const double e1 = c->E_state, e0 = c->sa_eng;
+                if (e1 < 100.0 * p.eta || fabs((e0 - e1) / e0) < 0.02) {
+                    c->done = 1;
+                    c->status = ST_CONVERGED;
+                    return;
+                }
+                c->sa_eng = e1;
+            }
+            if (count % 10 == 0) c->dt *= 2.0;
+        }
+        c->fill_slot = -1;
+        return;
+    }
     if (!raw && c->grow_pending) {
         const double d0 = c->dt;
         c->dt = (d0 * p.cap_probe < p.dt_cap) ? d0 * p.grow_factor : p.dt_cap;
@@ -183,6 +208,27 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     const Scal cs = c->sc[R_CAND];
     const double E1 = cs.E;
     c->E_last_attempt = E1;
+    if (p.sched == SCHED_SHAPE) {
+        // belastic.cpp:245-262: keep the attempt only if the energy fell strictly
+        // (a non-finite attempt never does); otherwise halve dt, ending below dt_min
+        if (!(E1 < c->E_state)) {
+            c->dt *= 0.5;
+            c->rejects++;
+            c->fresh = 0;
+            if (c->dt < p.dt_min) { c->done = 1; c->status = ST_DT_UNDERFLOW; }
+            return;
+        }
+        c->spec_state ^= 1;
+        c->part_state ^= 1;
+        c->ab_state ^= 1;
+        c->sc[R_STATE] = cs;
+        c->E_state = E1;
+        c->fresh = 1;
+        c->steps++;
+        c->grow_pending = 1;  // the loop head runs before the next attempt
+        if (c->steps >= c->target) { c->done = 1; c->status = ST_TARGET; }
+        return;
+    }
     if (!raw) {
         if (p.adaptive) {
             if (E1 > c->E_state + p.reject_tol * fabs(c->E_state)) {

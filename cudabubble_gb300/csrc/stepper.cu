@@ -148,6 +148,10 @@ int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double be
     CB_H(h);
     return h->impl->set_loop_state(t, dt, alpha, beta);
 }
+int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st) {
+    CB_H(h);
+    return h->impl->shape_adjust(max_steps, st);
+}
 int cb_synchronize(cb_handle* h) { CB_H(h); return h->impl->sync(); }
 int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts) {
     CB_H(h);

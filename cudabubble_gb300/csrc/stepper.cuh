@@ -204,6 +204,7 @@ struct Handle {
     virtual int field(int which, double* out, bool dev) = 0;
     virtual int set_dt(double dt) = 0;
     virtual int set_loop_state(double t, double dt, double alpha, double beta) = 0;
+    virtual int shape_adjust(int max_steps, cb_adjust_stats* st) = 0;
     virtual int sync() = 0;
     virtual long long bytes() const = 0;
     virtual int run_timed(int nsteps, long long flush_bytes, double* ms, int* attempts) = 0;
@@ -367,6 +368,7 @@ template <class T> class Stepper final : public Handle {
         if (st) cudaStreamSynchronize(st);
         if (g_loop) cudaGraphExecDestroy(g_loop);
         if (g_raw) cudaGraphExecDestroy(g_raw);
+        if (g_shape) cudaGraphExecDestroy(g_shape);
         cudaFree(arena);
         cudaFree(scratch);
         cudaFree(cbuf);
@@ -592,6 +594,114 @@ template <class T> class Stepper final : public Handle {
 
     int sync() override {
         CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    // belastic::shape_adjust (belastic.cpp:174-284): forward Euler on g0 alone
+    // from the current state, under the adjustment's accept and dt rules
+    // (SCHED_SHAPE in the prologue and decide kernels).  It runs the Euler
+    // attempt of this precision with M1 = M2 = 0 and ga = 3 / eta, so that
+    // phi' = phi - dt ga (eta g0) = phi - 3 dt g0 and the energy is eta E_el.
+    // The loop's own dt, time and counters are kept (belastic.cpp:280: the
+    // adjustment restores time_step and does not advance time_current).  The
+    // volume and area targets are taken again from the adjusted state when the
+    // handle takes them from the state (beta <= 0): run_static_fEIF and
+    // run_static read them after the adjustment (belastic.cpp:558-591, :289-325).
+    int shape_adjust(int max_steps, cb_adjust_stats* out) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        if (!(p.eta > 0)) return fail(CB_EINVAL, "shape adjustment needs eta > 0");
+        if (max_steps < 0) return fail(CB_EINVAL, "max_steps < 0");
+        cb_params u = up;
+        u.method = CB_EULER;
+        u.M1 = u.M2 = 0.0;
+        u.ga = 3.0 / p.eta;
+        u.fixed_time_step = 0.0;
+        u.rel_tol = 0.0;
+        u.reject_tol = 0.0;
+        Eff es{};
+        int rc = make_params(u, es);
+        if (rc) return rc;
+        Params ps = es.p;
+        ps.sched = SCHED_SHAPE;
+        ps.dt_min = 1e-13;  // belastic.cpp:260
+        CB_CK(pull());
+        const Ctrl saved = hc;
+        CB_CK(cudaMemcpyAsync(&d->p, &ps, sizeof ps, cudaMemcpyHostToDevice, st));
+        // the state's sums and, in the FP32 form, its Euler partials (G slot)
+        if (sizeof(T) == 4) CB_CK(xypass(XY_FUSED, R_STATE));
+        CB_CK(pull());
+        const double E_start = p.eta * hc.sc[R_STATE].E_el;
+        hc.sc[R_STATE].E = E_start;
+        hc.E_state = hc.E_init = hc.sa_eng = E_start;
+        hc.dt = 1e-7;  // belastic.cpp:185
+        hc.t = 0.0;
+        hc.steps = hc.attempts = hc.rejects = 0;
+        hc.target = max_steps > 0 ? max_steps : 1000000;
+        hc.done = 0;
+        hc.status = ST_RUNNING;
+        hc.grow_pending = 1;  // the loop head runs before the first attempt
+        hc.fresh = 1;
+        hc.nonfinite = 0;
+        CB_CK(push());
+        if (!g_shape) {
+            rc = capture(false, &g_shape, M_EULER);
+            if (rc) {
+                cudaMemcpy(&d->p, &p, sizeof p, cudaMemcpyHostToDevice);
+                return rc;
+            }
+        }
+        cudaEvent_t e0, e1;
+        CB_CK(cudaEventCreate(&e0));
+        CB_CK(cudaEventCreate(&e1));
+        CB_CK(cudaEventRecord(e0, st));
+        long long launches = 0;
+        const long long limit = 70LL * (hc.target + 1LL) + 1000;
+        while (!hc.done && launches <= limit) {
+            for (int i = 0; i < 64; ++i) CB_CK(cudaGraphLaunch(g_shape, st));
+            launches += 64;
+            CB_CK(pull());
+        }
+        CB_CK(cudaEventRecord(e1, st));
+        CB_CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const Ctrl fin = hc;
+        // back to the loop: its parameters, counters and dt, on the adjusted state
+        CB_CK(cudaMemcpyAsync(&d->p, &p, sizeof p, cudaMemcpyHostToDevice, st));
+        hc = saved;
+        hc.spec_state = fin.spec_state;
+        hc.part_state = fin.part_state;
+        hc.ab_state = fin.ab_state;
+        hc.sc[R_STATE] = fin.sc[R_STATE];
+        hc.fresh = 1;
+        hc.done = 0;
+        CB_CK(push());
+        CB_CK(xypass(sizeof(T) == 4 ? XY_FUSED : XY_REDUCE_FULL, R_STATE));
+        CB_CK(pull());
+        if (!(up.beta > 0.0)) {
+            hc.alpha = hc.alpha0 = hc.sc[R_STATE].V;
+            hc.beta = hc.beta0 = hc.sc[R_STATE].S;
+        }
+        Scal& sc = hc.sc[R_STATE];
+        const double ve = sc.V - hc.alpha, se = sc.S - hc.beta;
+        sc.E = p.eta * sc.E_el + 0.5 * p.M1 * ve * ve + 0.5 * p.M2 * se * se;
+        hc.E_state = hc.E_init = sc.E;
+        CB_CK(push());
+        CB_CK(Launch<T>::coef(d, 1, e.accurate, st));
+        CB_CK(cudaStreamSynchronize(st));
+        if (out) {
+            out->steps = fin.steps;
+            out->attempts = fin.attempts;
+            out->status = fin.done ? fin.status : ST_RUNNING;
+            out->graph_launches = (int)launches;
+            out->t = fin.t;
+            out->E_start = E_start;
+            out->E_end = fin.E_state;
+            out->device_ms = ms;
+        }
+        if (!fin.done) return fail(CB_ENOTCONVERGED, "shape adjustment made no progress after %lld attempts", launches);
         return CB_OK;
     }
 
@@ -956,15 +1066,17 @@ template <class T> class Stepper final : public Handle {
         return CB_OK;
     }
     // prof != nullptr: record an event pair around every launch (profiling; not captured)
-    int enqueue_attempt(bool raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
-        cudaError_t r = enqueue_group<T>(p.method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw, p.split, st, prof);
+    int enqueue_attempt(bool raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr,
+                        int method = -1) {
+        cudaError_t r = enqueue_group<T>(method < 0 ? p.method : method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw,
+                                         p.split, st, prof);
         if (r != cudaSuccess) return fail(CB_ECUDA, "enqueue attempt: %s", cudaGetErrorString(r));
         return CB_OK;
     }
-    int capture(bool raw, cudaGraphExec_t* out) {
+    int capture(bool raw, cudaGraphExec_t* out, int method = -1) {
         cudaGraph_t g = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_attempt(raw);
+        int rc = enqueue_attempt(raw, nullptr, method);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -995,7 +1107,7 @@ template <class T> class Stepper final : public Handle {
     cudaStream_t st = nullptr;
     InstT<double>* aux = nullptr;  // FP64 descriptor for exact set/get of phi (FP32 form)
     InstT<double> aux_h{};
-    cudaGraphExec_t g_loop = nullptr, g_raw = nullptr;
+    cudaGraphExec_t g_loop = nullptr, g_raw = nullptr, g_shape = nullptr;
     void* flush_buf = nullptr;
     long long flush_size = 0;
     bool have_state = false;

@@ -13,7 +13,9 @@ and ``belastic::run_static_fEIF``, ``belastic.cpp:554-786``):
 * starts from ``d<nx>x<ny>x<nz>.out`` when ninit is 7 and otherwise from the
   workload ellipsoid (a = b = 1.6, c = 0.8), standing in for the reference's
   hard-coded shapes, which are outside this stepper's scope;
-* resumes from ``<nx>x<ny>x<nz>.info`` (time, dt, alpha, beta) when present;
+* resumes from ``<nx>x<ny>x<nz>.info`` (time, dt, alpha, beta) when present,
+  and otherwise runs the shape adjustment first when the ini's shape flag
+  (field 8) is nonzero (``belastic.cpp:558-560``);
 * writes the reference's outputs at the start, every ``--output-seconds`` of
   wall time (20 s as ``belastic.cpp:759``) and at exit: the ``vol_sur``,
   ``lamb``, ``error``, ``time_step``, ``alpha_beta`` and ``energy`` logs,
@@ -49,6 +51,7 @@ class Run:
         fields = self.line.split()
         self.ifold = int(fields[0])
         self.ninit = int(fields[11]) if len(fields) > 11 else 0
+        self.b_shape = int(fields[7]) if len(fields) > 7 else 0
         self.params = capi.params_from_ini(self.line)
         p = self.params
         self.shape = (p.nz, p.ny, p.nx)
@@ -127,6 +130,17 @@ class Run:
         self.say(f"vol: {v:12.7f} surf: {s:12.7f} eng: {eng:12.10f} Error: {err:12.10f} "
                  f"Time_step: {sc['dt']:e}\n")
 
+    def shape_adjust(self, st) -> None:
+        """belastic::shape_adjust's messages (belastic.cpp:197-283) around the
+        device loop; the energies of its intermediate checks are not reported."""
+        self.say("Start Shape Adjusting......\n")
+        r = st.shape_adjust()
+        self.say(f"Start energy is {r['E_start']:12.8f}\n")
+        self.say(f"energy is {r['E_end']:12.8f}\n")
+        if r["status"] == capi.CB_DONE_DT_UNDERFLOW:
+            self.say("time_step in shape adjust < 1e-13, get exit.\n")
+        self.say("Shape Adjust Ended successfully\n")
+
     def run(self, max_steps: int = 0) -> int:
         p = self.params
         info = checkpoint.read_info(self.folder, self.shape)
@@ -138,6 +152,8 @@ class Run:
             self.alpha3 = info["alpha3"]
         st = capi.Stepper(p)
         st.set_phi(self.initial_phi())
+        if info is None and self.b_shape != 0:  # belastic.cpp:558-560 (a new run only)
+            self.shape_adjust(st)
         if info is not None:
             alpha, beta = info["alpha"], info["beta"]
             if beta <= 0.0:  # belastic.cpp:588-591: targets from the state

@@ -119,6 +119,17 @@ typedef struct cb_run_stats {
     double device_ms;        /* CUDA-event time of the call's device work */
 } cb_run_stats;
 
+typedef struct cb_adjust_stats {
+    int steps;               /* accepted adjustment steps */
+    int attempts;            /* attempts (accepted + rejected) */
+    int status;              /* CB_DONE_CONVERGED (energy below 100 eta or changed < 2 % between
+                                checks), CB_DONE_DT_UNDERFLOW (dt < 1e-13) or CB_DONE_TARGET */
+    int graph_launches;
+    double t;                /* adjustment time reached (not added to the run's time) */
+    double E_start, E_end;   /* unconstrained energy eta E_el before and after */
+    double device_ms;
+} cb_adjust_stats;
+
 typedef struct cb_handle cb_handle;
 
 /* defaults for every field (FP64 ETD4 on 64^3, the reference's main path) */
@@ -155,6 +166,14 @@ int cb_set_dt(cb_handle* h, double dt);
  * reference run (the .info file of fluidbase::load_info, fluidbase.cpp:2797-2826);
  * call after cb_set_phi, which otherwise takes alpha, beta from the new state */
 int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double beta);
+/* belastic::shape_adjust (belastic.cpp:174-284): unconstrained pre-relaxation of the
+ * current state, phi <- phi - 3 dt g0, kept only where eta E_el falls strictly, dt
+ * from 1e-7 (halved on a rise, doubled every 10 steps); ends when eta E_el < 100 eta,
+ * when it changed by < 2 % since the last check (checks at multiples of 1e-4 of
+ * adjustment time), or when dt < 1e-13.  The loop's dt, time and counters are kept;
+ * alpha, beta are taken again from the adjusted state when the parameters' beta <= 0.
+ * max_steps > 0 bounds the accepted steps (0: 1,000,000). */
+int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st);
 int cb_synchronize(cb_handle* h);
 /* HBM bytes held by the handle's stepping state */
 long long cb_handle_bytes(cb_handle* h);

@@ -522,6 +522,63 @@ class Belastic:
                 callback(self)
         return "max_steps"
 
+    def shape_adjust(self, max_steps: int = 0, log=None):
+        """Unconstrained pre-relaxation, belastic.cpp:174-284.
+
+        Forward Euler on g0 alone, phi <- phi - 3 dt g0 (:245-246), from dt =
+        1e-7 (:185).  An attempt is kept only if the unconstrained energy
+        eta E_el falls strictly (:249); otherwise phi is restored and dt halved
+        (:254-258), and the run ends once dt < 1e-13 (:260, :263-268).  The
+        loop head advances tcur by dt and counts the step (:204-207); when dt
+        > 1e-4 or int(tcur/dt) is a multiple of int(1e-4/dt) (:215) it ends if
+        the energy is below 100 eta or moved by less than 2 % since the last
+        such check (:223); every 10th count doubles dt (:231-233).  The
+        reference's blow-up test reads a host copy of phi that this loop never
+        updates (:270), so it never fires and is left out; a non-finite
+        attempt fails the strict-decrease test and is rejected.
+
+        Returns (reason, accepted steps, attempts, tcur).  The caller's dt is
+        untouched (:280) and tcur is not added to the run's time."""
+        eta = self.p.eta
+        pd = self.pd
+        dt = 1e-7
+        tcur = 0.0
+        steps = 1
+        eng0 = self.getstaticenergy(pd, False)
+        eng = eng0
+        accepted = attempts = 0
+        while True:
+            tcur += dt
+            steps += 1
+            if dt > 1e-4 or int(tcur / dt) % int(1e-4 / dt) == 0:
+                eng1 = self.getstaticenergy(pd, False)
+                if log is not None:
+                    log(eng1)
+                if eng1 < 100 * eta or abs((eng - eng1) / eng) < 0.02:
+                    return "converged", accepted, attempts, tcur
+                eng = eng1
+            if steps % 10 == 0:
+                dt *= 2.0
+            od = pd.d.copy()
+            g0 = pd.g0().copy()
+            while True:
+                attempts += 1
+                pd.time_diff_solve_phi(g0, -dt * 3.0)
+                eng1 = self.getstaticenergy(pd, False)
+                if eng1 < eng0:
+                    eng0 = eng1
+                    break
+                pd.d = od.copy()
+                pd.update_d()
+                dt /= 2.0
+                if dt < 1e-13:
+                    break
+            if dt < 1e-13:
+                return "dt_underflow", accepted, attempts, tcur
+            accepted += 1
+            if max_steps and accepted >= max_steps:
+                return "max_steps", accepted, attempts, tcur
+
     def scalars(self):
         pd = self.pd
         return dict(V=pd.vol(), S=pd.surface(), E_el=pd.elastic_eng(),

@@ -12,8 +12,12 @@
 // call inside them is the reference's own (ETD2RK, ETD4RK,
 // get_sum_fgqterm, time_diff_solve_phi, getstaticenergy, vol, surface).
 //
+// The adjust mode calls the reference's own belastic::shape_adjust()
+// (belastic.cpp:174-284) once and dumps the relaxed phi.
+//
 // usage:
 //   refstep fields <workdir> <nx> <nz> <epssize> <dt> <phi0.out> <outdir>
+//   refstep adjust <workdir> <nx> <nz> <epssize> <phi0.out> <outdir>
 //   refstep run    <workdir> <euler|etd2|etd4> <nx> <nz> <epssize> <time_step>
 //                  <fixed_dt> <M1> <M2> <nsteps> <phi0.out> <outdir> <snap_every>
 // Standard headers first: the reference's tool.h defines min/max macros.
@@ -319,10 +323,44 @@ static int mode_run(int argc, char** argv) {
     return 0;
 }
 
+static int mode_adjust(int argc, char** argv) {
+    if (argc < 8) die("adjust args");
+    const char* workdir = argv[2];
+    int nx = atoi(argv[3]), nz = atoi(argv[4]), epssize = atoi(argv[5]);
+    size_t n = (size_t)nx * nx * nz;
+    std::vector<double> phi0 = read_raw(argv[6], n);
+    std::string out = argv[7];
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) die("getcwd");
+    if (out[0] != '/') out = std::string(cwd) + "/" + out;
+    stage_workdir(workdir, nx, nz, epssize, 1e-6, 0.0, 1e4, 1e4, phi0);
+
+    belastic t(0);
+    phasefield* pd = t.m_pd;
+    const double E0 = t.getstaticenergy(pd, false);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0);
+    t.shape_adjust();  // the reference's own loop; its messages go to stdout
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    dump_dev(out + "/phi_adjust.bin", pd->d(), n * 8);
+    const double V = dget(pd->vol()), S = dget(pd->surface()), Eel = dget(pd->elastic_eng());
+    FILE* js = fopen((out + "/scalars.json").c_str(), "w");
+    fprintf(js, "{\"E0\": %.17g, \"E\": %.17g, \"E_el\": %.17g, \"V\": %.17g, \"S\": %.17g, \"dt\": %.17g, \"ms\": %.6f}\n",
+            E0, t.getstaticenergy(pd, false), Eel, V, S, t.time_step, ms);
+    fclose(js);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) die("mode");
     if (!strcmp(argv[1], "fields")) return mode_fields(argc, argv);
     if (!strcmp(argv[1], "run")) return mode_run(argc, argv);
+    if (!strcmp(argv[1], "adjust")) return mode_adjust(argc, argv);
     die("unknown mode");
     return 2;
 }

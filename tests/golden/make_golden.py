@@ -44,6 +44,8 @@ def phi0_for(case: dict) -> np.ndarray:
     shape = case.get("shape", "fixed")
     if shape == "fixed":
         return ellipsoid_phi0(nx, nz, eps, (1.6, 1.6, 0.8))
+    if shape == "wide":  # a profile wider than the equilibrium tanh: its energy starts high
+        return ellipsoid_phi0(nx, nz, eps * case["width"], (1.6, 1.6, 0.8))
     rng = np.random.default_rng(case["seed"])
     ax = seeded_axes(rng)
     if shape == "seeded":
@@ -86,13 +88,20 @@ RUN_CASES = [
          M=1e4, nsteps=20, snap=0, shape="two", seed=3),
 ]
 
+# the unconstrained pre-relaxation belastic::shape_adjust (belastic.cpp:174-284), run
+# once by the reference itself; the wide profiles start above its 100 eta exit energy
+ADJUST_CASES = [
+    dict(name="adjust32", nx=32, nz=32, epssize=200, shape="wide", width=2.0),
+    dict(name="adjust48", nx=48, nz=48, epssize=150, shape="wide", width=3.0),
+]
+
 
 def cmd_run(out: str, only: list[str] | None):
     os.makedirs(out, exist_ok=True)
     # the reference writes its ini, phi0 copy and logs into a work tree; keep
     # that (and large phi0 files) out of the result directory
     work = os.path.join(tempfile.mkdtemp(prefix="cbref_"), "w")
-    for case in FIELD_CASES + RUN_CASES:
+    for case in FIELD_CASES + RUN_CASES + ADJUST_CASES:
         if only and case["name"] not in only:
             continue
         d = os.path.join(out, case["name"])
@@ -104,6 +113,9 @@ def cmd_run(out: str, only: list[str] | None):
         if case in FIELD_CASES:
             args = [REFSTEP, "fields", work + "_" + case["name"], str(case["nx"]), str(case["nz"]),
                     str(case["epssize"]), repr(case["dt"]), p0, d]
+        elif case in ADJUST_CASES:
+            args = [REFSTEP, "adjust", work + "_" + case["name"], str(case["nx"]), str(case["nz"]),
+                    str(case["epssize"]), p0, d]
         else:
             args = [REFSTEP, "run", work + "_" + case["name"], case["method"], str(case["nx"]),
                     str(case["nz"]), str(case["epssize"]), repr(case["time_step"]), repr(case["fixed"]),
@@ -124,8 +136,14 @@ def _read(path, dtype, shape):
 def cmd_pack(raw: str, dest: str):
     manifest = {"generator": "tests/golden/make_golden.py", "reference": "mrazizadeh/CudaBubble (FP64 cuFFT build)",
                 "cases": {}}
+    old = os.path.join(dest, "manifest.json")
+    if os.path.exists(old):  # a partial run (--only) updates its own cases and keeps the rest
+        with open(old) as f:
+            manifest["cases"] = json.load(f).get("cases", {})
     for case in FIELD_CASES:
         d = os.path.join(raw, case["name"])
+        if not os.path.isdir(d):
+            continue
         nx, nz = case["nx"], case["nz"]
         shp, shc = (nz, nx, nx), (nz, nx, nx // 2 + 1)
         arrs = {"phi0": _read(os.path.join(d, case["name"] + "_phi0.bin"), np.float64, shp)}
@@ -156,6 +174,18 @@ def cmd_pack(raw: str, dest: str):
             np.savez_compressed(os.path.join(dest, case["name"] + ".npz"), **snaps)
             entry["snapshots"] = sorted(snaps)
         manifest["cases"][case["name"]] = entry
+    for case in ADJUST_CASES:
+        d = os.path.join(raw, case["name"])
+        if not os.path.isdir(d):
+            continue
+        nx, nz = case["nx"], case["nz"]
+        phi = _read(os.path.join(d, "phi_adjust.bin"), np.float64, (nz, nx, nx))
+        np.savez_compressed(os.path.join(dest, case["name"] + ".npz"), phi_adjust=phi)
+        with open(os.path.join(d, "scalars.json")) as f:
+            sc = json.load(f)
+        # the reference's own messages: "energy is %12.8f" at each convergence check
+        checks = [float(l.split()[-1]) for l in open(os.path.join(d, "log.txt")) if l.startswith("energy is")]
+        manifest["cases"][case["name"]] = dict(case, scalars=sc, checks=checks)
     with open(os.path.join(dest, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
     print("packed", sorted(manifest["cases"]))

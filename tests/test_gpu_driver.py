@@ -53,3 +53,34 @@ def test_driver_outputs_and_resume(cblib, tmp_path):
     E2 = float(open(os.path.join(fold, "energy32x32x32.txt")).readlines()[-1].split(",")[4])
     assert E2 == pytest.approx(want_E, abs=2e-5)  # the log keeps 5 decimals
     assert info2["time_current"] > info["time_current"]
+
+
+def test_driver_shape_adjust_on_new_run(cblib, tmp_path):
+    """A new run with a nonzero shape flag (ini field 8) relaxes the start shape
+    first (belastic.cpp:558-560); a resumed run does not."""
+    from cudabubble_gb300 import capi, checkpoint, driver
+    res = str(tmp_path)
+    line = _ini(9, 2).split()
+    line[7] = "1"
+    (tmp_path / "ini0.dat").write_text(" ".join(line) + "\n")
+    driver.Run(res, 0, output_seconds=1e9).run(max_steps=16)
+    fold = os.path.join(res, "9")
+    out = open(os.path.join(fold, "output32x32x32.txt")).read()
+    assert "Start Shape Adjusting" in out and "Shape Adjust Ended successfully" in out
+    d16 = checkpoint.read_out(fold, "d", (32, 32, 32))
+
+    p = capi.params_from_ini(" ".join(line))
+    st = capi.Stepper(p)
+    st.set_phi(driver.Run(res, 0).initial_phi())
+    a = st.shape_adjust()
+    assert a["steps"] > 0 and a["E_end"] < a["E_start"]
+    st.run(16)
+    assert np.abs(st.get_phi() - d16).max() < 1e-12
+    st.close()
+
+    # resuming from the .info file skips the adjustment
+    line[11] = "7"
+    (tmp_path / "ini0.dat").write_text(" ".join(line) + "\n")
+    driver.Run(res, 0, output_seconds=1e9).run(max_steps=4)
+    out2 = open(os.path.join(fold, "output32x32x32.txt")).read()
+    assert out2.count("Start Shape Adjusting") == 1

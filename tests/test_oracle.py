@@ -203,3 +203,38 @@ def test_oracle_trajectories_match_reference(name, tol):
     err = np.abs(b.pd.d - snaps[key]).max()
     assert err < tol, err
     assert b.getstaticenergy(b.pd) == pytest.approx(last["E"], rel=1e-11 if tol <= 1e-10 else 3e-4)
+
+
+# (case, max |phi - phi_ref|, relative energy tolerance).  The adjustment drives
+# dt to the explicit-Euler stability limit and keeps it there, so the unstable
+# high-|k| modes amplify each implementation's FP64 rounding step after step:
+# ~1e-10 in phi after the 86 steps of adjust32 and ~1e-8 after the 820 of
+# adjust48, with the same accept / reject decisions and the same checks.
+ADJUST_CASES = [("adjust32", 5e-10, 1e-10), ("adjust48", 5e-8, 1e-7)]
+
+
+@pytest.mark.parametrize("name,phi_tol,e_tol", ADJUST_CASES)
+def test_oracle_shape_adjust_matches_reference(name, phi_tol, e_tol):
+    """The restated shape_adjust (belastic.cpp:174-284) against the reference's
+    own run of it: the relaxed field, the final energy, and the energy the
+    reference printed at each convergence check ("energy is %12.8f")."""
+    man = _manifest()
+    if name not in man["cases"]:
+        pytest.skip(f"golden case {name} not generated")
+    case = man["cases"][name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    nx, nz = case["nx"], case["nz"]
+    eps = O.eps_from_epssize(case["epssize"], 2 * math.pi, nx)
+    phi0 = O.ellipsoid_phi0(nx, nz, eps * case["width"], (1.6, 1.6, 0.8))
+    b = O.Belastic(O.Params(nx=nx, nz=nz, eps=eps), phi0)
+    assert b.getstaticenergy(b.pd, False) == pytest.approx(case["scalars"]["E0"], rel=1e-12)
+    checks = []
+    why, accepted, attempts, _ = b.shape_adjust(log=checks.append)
+    assert why == "converged" and accepted > 0
+    # the reference prints the start energy line as "Start energy is", then one
+    # "energy is" line per check, the last being the one that ended the loop
+    assert len(checks) == len(case["checks"])
+    assert checks == pytest.approx(case["checks"], rel=e_tol, abs=1e-8)  # printed with 8 decimals
+    err = np.abs(b.pd.d - g["phi_adjust"]).max()
+    assert err < phi_tol, err
+    assert b.getstaticenergy(b.pd, False) == pytest.approx(case["scalars"]["E"], rel=e_tol)
