@@ -159,10 +159,12 @@ def algorithmic_bytes(n: int, fsize: int, att: int, rej: int):
     """Bytes each kernel kind must move over `att` attempts with `rej` retries
     (a retry skips the stage-1 nonlinear pass and reuses the stored N_u).
     F = one half-spectrum field of complex FP32 (8 B per mode); the stepped
-    state fields (phi-hat, candidate, a-hat) are double-float pairs, 2F."""
+    state fields (phi-hat, candidate, a-hat) are double-float pairs, 2F, and so
+    is the real-space u (n^3 points of 8 B, counted as 2F)."""
     F = n * n * (n // 2 + 1) * 2 * fsize
     return {
-        "xy_fused": att * 2 * 4 * F,                    # per stage: read P0, P2; write G'', w
+        # per stage: read P0, P2, u_state (2F); write G'', w; the candidate also writes its u (2F)
+        "xy_fused": att * (2 * 6 * F + 2 * F),
         # S2: read A, B, a-hat(2F), phi(2F), N_u; write phi'(2F), P0, P2 = 11F
         # S1 fresh: read G'', w, phi(2F); write N_u, a-hat(2F), P0, P2   = 9F
         # S1 retry: read N_u, phi(2F); write a-hat(2F), P0, P2           = 7F

@@ -36,7 +36,10 @@ struct Scal {
     double grad2;   // mean |grad u|^2 via Parseval over the half spectrum
     double lsq;     // mean R^2 of the Euler right-hand side (LSerror) via Parseval
     double V, S, E_el, E;
-    double pad[3];
+    // FP32 form: FP64 totals of the fused pass's real-space partials G'' and w,
+    // the exact k = 0 modes of their transforms (z pass)
+    double sum_g, sum_h;
+    double pad;
 };
 
 struct Ctrl {
@@ -60,6 +63,7 @@ struct Ctrl {
     int nonfinite;
     int grow_pending;  // apply the dt growth rule at the start of the next attempt
     int ab_state;      // FP32 form: G[ab_state] holds the state's fused-pass outputs
+    int u_state;       // FP32 form: U[u_state] holds the state's real-space field
     int tab_cur;       // coefficient table of the current dt
     int tab_next;      // round-robin slot for the next new dt
     int fill_slot;     // table being filled this attempt (-1: none)
@@ -138,6 +142,12 @@ template <class T> struct InstT {
     void* B;
     void* Y[2];       // split plane path: y-transformed fields (nullptr when unused)
     void* G[2][2];    // FP32 form: XY_FUSED outputs (G'', w) of the state / candidate (ctrl->ab_state)
+    // FP32 form: real-space u of the state / candidate as double-float pairs
+    // [z][y][x] (ctrl->u_state).  The z pass transforms only u - u_state, and the
+    // fused pass adds it to U[u_state]: u from a plain FP32 transform carries
+    // ~6e-8 absolute error, which where u = +-1 + d with d below it makes
+    // w = u^3 - u ~ +-2 d wrong by 100 %, with one sign over the whole far field
+    void* U[2];
     T* coef;          // kNTab tables of (kmax + 1) * 8 entries
     Ctrl* ctrl;
     double* part_xy;  // [nz][4] per-plane partial sums

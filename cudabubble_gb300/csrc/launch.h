@@ -32,5 +32,7 @@ template <class T> struct Launch {
 
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,
                              const double* d, double eps, double x0, double x1, double x2, cudaStream_t s);
+// real FP64 field -> double-float pairs (hi = fl32(v), lo = fl32(v - hi)), n points
+cudaError_t launch_real_to_ff(const double* in, void* out, size_t n, cudaStream_t s);
 
 }  // namespace cb

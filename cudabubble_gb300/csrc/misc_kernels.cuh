@@ -221,6 +221,7 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
         c->spec_state ^= 1;
         c->part_state ^= 1;
         c->ab_state ^= 1;
+        c->u_state ^= 1;
         c->sc[R_STATE] = cs;
         c->E_state = E1;
         c->fresh = 1;
@@ -254,6 +255,7 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     c->spec_state ^= 1;
     c->part_state ^= 1;
     c->ab_state ^= 1;  // FP32 form: the candidate's fused-pass outputs become the state's
+    c->u_state ^= 1;   // and its real-space field
     c->sc[R_STATE] = cs;
     if (!raw && p.corr) {  // the energy against the corrected targets (belastic.cpp:68-86)
         const double ve = cs.V - c->alpha, se = cs.S - c->beta;

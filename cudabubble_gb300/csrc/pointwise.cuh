@@ -115,4 +115,38 @@ __device__ __forceinline__ void fused_point(const PC<T>& k, bool euler, T u, T l
     }
 }
 
+// FP32 form: u = U + v as a double-float pair, U = (hi, lo) the state's real-space
+// field and v the FP32 transform of u - u_state (TwoSum, then FastTwoSum)
+__device__ __forceinline__ float2 ff_add_f(float2 U, float v) {
+    const float s = U.x + v;
+    const float bp = s - U.x;
+    const float e = ((U.x - (s - bp)) + (v - bp)) + U.y;
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+
+// XY_FUSED point of the FP32 form from u = uh + ul.  u^2 - 1 is formed as
+// (uh - s)(uh + s) + 2 uh ul with s = +-1: uh - s is exact where |uh| is within a
+// factor 2 of 1, so u^2 - 1 and w = (u^2 - 1) u keep their relative accuracy where
+// u = +-1 + d with d far below FP32's spacing at 1; elsewhere u^2 - 1 is O(1) and
+// plain FP32 rounding is enough.  Otherwise as fused_point<float>.
+__device__ __forceinline__ void fused_point_u(const PC<float>& k, bool euler, float uh, float ul, float lap,
+                                              Acc<float>& as, Acc<float>& af, float& g, float& h) {
+    const float D = 1.5f;
+    const float sg = uh < 0.f ? -1.f : 1.f;
+    const float u2m = fmaf(uh - sg, uh + sg, 2.f * uh * ul);
+    const float u2 = u2m + 1.f;
+    const float w = u2m * uh;
+    const float f = k.k_ieps.mul(w) - k.k_eps.mul(lap);
+    as.add(u2m * u2m);
+    af.add(f * f);
+    if (euler) {
+        g = k.k_K2.mul((3.f * u2 - 1.f) * f);
+        h = f;
+    } else {
+        g = -(k.k_K3.mul(w) + k.k_K2.mul((3.f * u2 - D - 1.f) * f));
+        h = w;
+    }
+}
+
 }  // namespace cb

@@ -77,7 +77,9 @@ __global__ void __launch_bounds__(NT) ycol_kernel(const InstT<T>* __restrict__ i
             v = in0[(size_t)y * nc + kx];
             if (two) {
                 w = in1[(size_t)y * nc + kx];
-                if (inv) {  // laplacian partial Q = -cx (kx^2 + ky^2) P0 + P2 (Calc.cu:107-124)
+                // laplacian partial Q = -cx (kx^2 + ky^2) P0 + P2 (Calc.cu:107-124); in the FP32
+                // form's fused pass P2 is already the whole Laplacian (z_kernel.cuh)
+                if (inv && !(sizeof(T) == 4 && a.fused)) {
                     const int kyf = min(y, NY - y);
                     const int kk = kx * kx + kyf * kyf;
                     if constexpr (sizeof(T) == 8) {
@@ -239,21 +241,47 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
             __syncthreads();
         } else if (a.mode == XY_FUSED) {
             const bool euler = p.method == M_EULER;
-            Acc<T> as, af;
-            for (int it = tid; it < RPC * M; it += NT) {
-                const int q = it % M, j = it / M;
-                C* pu = S + j * LP + q;
-                C* pl = S + (RPC + j) * LP + q;
-                const C uu = *pu, ll = *pl;
-                C g, h;
-                fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
-                fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
-                *pu = g;
-                *pl = h;
+            Acc<T> as, af, ag, ah;
+            if constexpr (sizeof(T) == 4) {
+                // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
+                const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + row0 * M;
+                float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + row0 * M : nullptr;
+                for (int it = tid; it < RPC * M; it += NT) {
+                    const int q = it % M, j = it / M;
+                    const int ui = j * M + tidx<M>(q);  // row j, points 2m and 2m + 1
+                    const float4 Uv = __ldg(Us + ui);
+                    C* pu = S + j * LP + q;
+                    C* pl = S + (RPC + j) * LP + q;
+                    const C dd = *pu, ll = *pl;
+                    const float2 u0 = ff_add_f(make_float2(Uv.x, Uv.y), dd.x);
+                    const float2 u1 = ff_add_f(make_float2(Uv.z, Uv.w), dd.y);
+                    if (Uo) Uo[ui] = make_float4(u0.x, u0.y, u1.x, u1.y);
+                    C g, h;
+                    fused_point_u(k, euler, u0.x, u0.y, ll.x, as, af, g.x, h.x);
+                    fused_point_u(k, euler, u1.x, u1.y, ll.y, as, af, g.y, h.y);
+                    ag.add(g.x); ag.add(g.y);
+                    ah.add(h.x); ah.add(h.y);
+                    *pu = g;
+                    *pl = h;
+                }
+            } else {
+                for (int it = tid; it < RPC * M; it += NT) {
+                    const int q = it % M, j = it / M;
+                    C* pu = S + j * LP + q;
+                    C* pl = S + (RPC + j) * LP + q;
+                    const C uu = *pu, ll = *pl;
+                    C g, h;
+                    fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
+                    fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
+                    ag.add(g.x); ag.add(g.y);
+                    ah.add(h.x); ah.add(h.y);
+                    *pu = g;
+                    *pl = h;
+                }
             }
             auto pv = as.part();
-            decltype(pv) vv[2] = {pv, af.part()};
-            xy_sums_finalize<T>(I, ctrl, p, rb, nblk, vv, red, a.role, true);
+            decltype(pv) vv[4] = {pv, af.part(), ag.part(), ah.part()};
+            xy_sums_finalize<T, 4>(I, ctrl, p, rb, nblk, vv, red, a.role, true);
             __syncthreads();
         } else {
             const bool full = a.mode == XY_REDUCE_FULL;

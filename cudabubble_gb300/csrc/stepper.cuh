@@ -157,11 +157,9 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.dt_min = 1e-23;
     p.tmax = u.tmax >= 0 ? u.tmax : 4.0;
     p.rel_tol = u.rel_tol > 0 ? u.rel_tol : 0.0;
-    // the FP32 form's step-to-step energy changes carry FP32 transform noise of up to
-    // ~5e-6 relative late in a relaxation (high-|k| modes re-seeded each step); a rise
-    // below that is not one it can resolve, and rejecting on it halves dt on noise
-    // alone until dt underflows
-    p.reject_tol = u.reject_tol >= 0 ? u.reject_tol : (u.precision == CB_FP32 ? 1e-5 : 0.0);
+    // both forms default to the reference's strict E_new > E_old rejection
+    // (belastic.cpp:653-668); a positive reject_tol tolerates rises below reject_tol |E|
+    p.reject_tol = u.reject_tol >= 0 ? u.reject_tol : 0.0;
     // nonlinear term N-hat = A-hat + beta cx |k|^2 B-hat: beta = eta (Euler, -lap f in g0)
     // or -eta/eps (ETD, +lap t / eps in -eta NL)
     const double beta = euler ? p.eta : -p.eta / p.eps;
@@ -340,6 +338,8 @@ template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* l
     const size_t fs = al(ns * 16), fp = al(ns * sizeof(T) * 2);
     // Nu, P x6, A, B (+ Na, Nb), then the split path's Y0, Y1, then the FP32 form's G slots
     const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0) + (sizeof(T) == 4 ? 4 : 0);
+    // FP32 form: the state's and the candidate's real-space u, double-float
+    const size_t fu = sizeof(T) == 4 ? al((size_t)p.N * 8) : 0;
     // FP32 form: the FP64 plain transforms of set/get phi need their own Y0, Y1
     const int naux = (sizeof(T) == 4 && uses_split<double>(p)) ? 2 : 0;
     size_t off = 0;
@@ -347,6 +347,8 @@ template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* l
     off += (3 + naux) * fs;
     if (layout) layout[6] = off;
     off += nplain * fp;
+    if (layout) layout[8] = off;
+    off += 2 * fu;
     if (layout) layout[1] = off;
     off += al((size_t)kNTab * (p.kmax + 1) * 8 * sizeof(T));
     if (layout) layout[2] = off;
@@ -386,7 +388,7 @@ template <class T> class Stepper final : public Handle {
                         sizeof(T) == 4 ? "FP32" : "FP64");
         ns = (size_t)p.nz * p.ny * p.nc;
         ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
-        size_t lay[8];
+        size_t lay[9];
         arena_bytes = instance_arena_bytes<T>(p, lay);
         CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
@@ -406,8 +408,11 @@ template <class T> class Stepper final : public Handle {
         int nextf = nplain;
         if (uses_split<T>(p))
             for (int i = 0; i < 2; ++i) h.Y[i] = base + lay[6] + (nextf++) * fp;
-        if (sizeof(T) == 4)
+        if (sizeof(T) == 4) {
             for (int i = 0; i < 4; ++i) h.G[i / 2][i % 2] = base + lay[6] + (nextf++) * fp;
+            const size_t fu = ((size_t)p.N * 8 + 255) & ~(size_t)255;
+            for (int i = 0; i < 2; ++i) h.U[i] = base + lay[8] + i * fu;
+        }
         h.coef = reinterpret_cast<T*>(base + lay[1]);
         h.part_xy = reinterpret_cast<double*>(base + lay[2]);
         h.part_z = reinterpret_cast<double*>(base + lay[3]);
@@ -491,6 +496,8 @@ template <class T> class Stepper final : public Handle {
         }
         reset_ctrl();
         CB_CK(push());
+        // FP32 form: the state's real-space field, exact as a double-float pair
+        if (sizeof(T) == 4) CB_CK(launch_real_to_ff(src, h.U[0], (size_t)p.N, st));
         if (aux) {  // exact spectrum: FP64 transform into the 16 B/mode candidate field, then hi/lo split
             CB_CK(fwd3d_f64(src, h.spec[1], h.ahat));
             CB_CK(Launch<T>::f64_to_state(h.spec[1], h.spec[0], ns, 1, st));
@@ -628,7 +635,10 @@ template <class T> class Stepper final : public Handle {
         const Ctrl saved = hc;
         CB_CK(cudaMemcpyAsync(&d->p, &ps, sizeof ps, cudaMemcpyHostToDevice, st));
         // the state's sums and, in the FP32 form, its Euler partials (G slot)
-        if (sizeof(T) == 4) CB_CK(xypass(XY_FUSED, R_STATE));
+        if (sizeof(T) == 4) {
+            CB_CK(zpass(Z_INV_STATE, R_STATE));
+            CB_CK(xypass(XY_FUSED, R_STATE));
+        }
         CB_CK(pull());
         const double E_start = p.eta * hc.sc[R_STATE].E_el;
         hc.sc[R_STATE].E = E_start;
@@ -674,10 +684,12 @@ template <class T> class Stepper final : public Handle {
         hc.spec_state = fin.spec_state;
         hc.part_state = fin.part_state;
         hc.ab_state = fin.ab_state;
+        hc.u_state = fin.u_state;
         hc.sc[R_STATE] = fin.sc[R_STATE];
         hc.fresh = 1;
         hc.done = 0;
         CB_CK(push());
+        CB_CK(zpass(Z_INV_STATE, R_STATE));
         CB_CK(xypass(sizeof(T) == 4 ? XY_FUSED : XY_REDUCE_FULL, R_STATE));
         CB_CK(pull());
         if (!(up.beta > 0.0)) {

@@ -80,24 +80,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     // ---- load own packed columns (col 0 = kx 0 + i kx M) and the Laplacian partial
     for (int it = tid; it < NY * MH; it += NT) {
         const int cc = it % MH, ky = it / MH, c = c0 + cc;
+        // P0 holds u - u_state and P2 the whole Laplacian (z_kernel.cuh, FP32 form)
         const C v = __ldg(P0 + ky * NC + c), w = __ldg(P2 + ky * NC + c);
-        const int kyf = min(ky, NY - ky);
-        auto q = [&](C ww, C vv, int kk) {
-            if constexpr (sizeof(T) == 8) {
-                const T m2 = k.cx * (T)kk;
-                return cmk<C>(ww.x - m2 * vv.x, ww.y - m2 * vv.y);
-            } else {
-                return cmk<C>(ww.x - k.k_cx.mul((T)kk * vv.x), ww.y - k.k_cx.mul((T)kk * vv.y));
-            }
-        };
         if (c == 0) {
             const C vN = __ldg(P0 + ky * NC + M), wN = __ldg(P2 + ky * NC + M);
-            const C q0 = q(w, v, kyf * kyf), qN = q(wN, vN, M * M + kyf * kyf);
             S[ky * PY] = cmk<C>(v.x - vN.y, v.y + vN.x);
-            S[ky * PY + MH] = cmk<C>(q0.x - qN.y, q0.y + qN.x);
+            S[ky * PY + MH] = cmk<C>(w.x - wN.y, w.y + wN.x);
         } else {
             S[ky * PY + cc] = v;
-            S[ky * PY + MH + cc] = q(w, v, c * c + kyf * kyf);
+            S[ky * PY + MH + cc] = w;
         }
     }
     __syncthreads();
@@ -159,21 +150,32 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     // ---- sums and lambda-free partials G'', w of this CTA's rows
     {
         const bool euler = p.method == M_EULER;
-        Acc<T> as, af;
+        Acc<T> as, af, ag, ah;
+        // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
+        const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
+        float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
+                                      : nullptr;
         for (int it = tid; it < NH * M; it += NT) {
             const int qq = it % M, r = it / M;
+            const int ui = tidx<NY>(rank * NH + r) * M + tidx<M>(qq);  // row y, points 2m and 2m + 1
+            const float4 Uv = __ldg(Us + ui);
             C* pu = S + r * PX + qq;
             C* pl = pu + M;
-            const C uu = *pu, ll = *pl;
+            const C dd = *pu, ll = *pl;
+            const float2 u0 = ff_add_f(make_float2(Uv.x, Uv.y), dd.x);
+            const float2 u1 = ff_add_f(make_float2(Uv.z, Uv.w), dd.y);
+            if (Uo) Uo[ui] = make_float4(u0.x, u0.y, u1.x, u1.y);
             C g, h;
-            fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
-            fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
+            fused_point_u(k, euler, u0.x, u0.y, ll.x, as, af, g.x, h.x);
+            fused_point_u(k, euler, u1.x, u1.y, ll.y, as, af, g.y, h.y);
+            ag.add(g.x); ag.add(g.y);
+            ah.add(h.x); ah.add(h.y);
             *pu = g;
             *pl = h;
         }
         auto pv = as.part();
-        decltype(pv) vv[2] = {pv, af.part()};
-        xy_sums_finalize<T>(I, ctrl, p, 2 * z + rank, 2 * p.nz, vv, red, a.role, true);
+        decltype(pv) vv[4] = {pv, af.part(), ag.part(), ah.part()};
+        xy_sums_finalize<T, 4>(I, ctrl, p, 2 * z + rank, 2 * p.nz, vv, red, a.role, true);
         __syncthreads();
     }
 

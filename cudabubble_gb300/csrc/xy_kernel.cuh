@@ -37,6 +37,8 @@ __device__ __forceinline__ int part_set(const Ctrl* ctrl, int role) {
 __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* sums, int role, bool full) {
     const double ss = sums[1], sf = sums[2];
     Scal& s = ctrl->sc[role];
+    s.sum_g = sums[0];
+    s.sum_h = sums[3];
     const double c3 = 1.0606601717798212866;  // 3 / (2 sqrt 2)
     // V comes from the exact k = 0 mode the z pass stored in sum_u
     s.sum_s2 = ss;
@@ -50,20 +52,27 @@ __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* su
     }
 }
 
-// Per-CTA partial sums (slot `slot` of `nslots`) of (u^2 - 1)^2, f^2, then
-// the last CTA of the instance finalises the role's scalars; all threads call.
-template <class T, class V>
+// Per-CTA partial sums (slot `slot` of `nslots`) of (u^2 - 1)^2, f^2 and, with
+// NV = 4 (XY_FUSED), of the partials G'' and w; then the last CTA of the
+// instance finalises the role's scalars; all threads call.
+template <class T, int NV = 2, class V>
 __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Params& p, int slot, int nslots, V* vv,
                                         double* red, int role, bool full) {
-    double v[2];
-    block_sum<2>(vv, v, red);
+    static_assert(NV == 2 || NV == 4, "two or four sums");
+    double v[NV];
+    block_sum<NV>(vv, v, red);
     double* part = I.part_xy;
     int* last = reinterpret_cast<int*>(red + 128);
     if (threadIdx.x == 0) {
-        part[4 * slot + 0] = 0.0;
         part[4 * slot + 1] = v[0];
         part[4 * slot + 2] = v[1];
-        part[4 * slot + 3] = 0.0;
+        if constexpr (NV == 4) {
+            part[4 * slot + 0] = v[2];
+            part[4 * slot + 3] = v[3];
+        } else {
+            part[4 * slot + 0] = 0.0;
+            part[4 * slot + 3] = 0.0;
+        }
         __threadfence();
         const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[role], 1u);
         *last = done_blocks == (unsigned)(nslots - 1);
@@ -174,6 +183,9 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                         const T k2 = cx * (T)(c * c) + kyy;
                         S[ky * pitch + M + c] = cmk<C>(w.x - k2 * v.x, w.y - k2 * v.y);
                     }
+                } else if (a.mode == XY_FUSED) {  // P2 holds the whole Laplacian (z_kernel.cuh)
+                    if (c == 0) S[ky * pitch + M] = cmk<C>(w.x - wN.y, w.y + wN.x);
+                    else S[ky * pitch + M + c] = w;
                 } else {  // integer |k|^2 exact in FP32, cx folded hi + lo
                     const KC<T> kcx = PC<T>(p).k_cx;
                     auto q = [&](C ww, C vv, int kk) {
@@ -280,21 +292,48 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         } else if (a.mode == XY_FUSED) {
             // sums of the state and its lambda-free partials G'', w in one sweep
             const bool euler = p.method == M_EULER;
-            Acc<T> as, af;
-            for (int it = tid; it < NY * M; it += NT) {
-                const int q = it % M, r = it / M;
-                C* pu = S + r * pitch + q;
-                C* pl = pu + M;
-                const C uu = *pu, ll = *pl;
-                C g, h;
-                fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
-                fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
-                *pu = g;
-                *pl = h;
+            Acc<T> as, af, ag, ah;
+            if constexpr (sizeof(T) == 4) {
+                // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
+                const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
+                float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
+                                              : nullptr;
+                for (int it = tid; it < NY * M; it += NT) {
+                    const int q = it % M, r = it / M;
+                    const int ui = tidx<NY>(r) * M + tidx<M>(q);  // row y, points 2m and 2m + 1
+                    const float4 Uv = __ldg(Us + ui);
+                    C* pu = S + r * pitch + q;
+                    C* pl = pu + M;
+                    const C dd = *pu, ll = *pl;
+                    const float2 u0 = ff_add_f(make_float2(Uv.x, Uv.y), dd.x);
+                    const float2 u1 = ff_add_f(make_float2(Uv.z, Uv.w), dd.y);
+                    if (Uo) Uo[ui] = make_float4(u0.x, u0.y, u1.x, u1.y);
+                    C g, h;
+                    fused_point_u(k, euler, u0.x, u0.y, ll.x, as, af, g.x, h.x);
+                    fused_point_u(k, euler, u1.x, u1.y, ll.y, as, af, g.y, h.y);
+                    ag.add(g.x); ag.add(g.y);
+                    ah.add(h.x); ah.add(h.y);
+                    *pu = g;
+                    *pl = h;
+                }
+            } else {
+                for (int it = tid; it < NY * M; it += NT) {
+                    const int q = it % M, r = it / M;
+                    C* pu = S + r * pitch + q;
+                    C* pl = pu + M;
+                    const C uu = *pu, ll = *pl;
+                    C g, h;
+                    fused_point<T>(k, euler, uu.x, ll.x, as, af, g.x, h.x);
+                    fused_point<T>(k, euler, uu.y, ll.y, as, af, g.y, h.y);
+                    ag.add(g.x); ag.add(g.y);
+                    ah.add(h.x); ah.add(h.y);
+                    *pu = g;
+                    *pl = h;
+                }
             }
             auto pv = as.part();
-            decltype(pv) vv[2] = {pv, af.part()};
-            xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, true);
+            decltype(pv) vv[4] = {pv, af.part(), ag.part(), ah.part()};
+            xy_sums_finalize<T, 4>(I, ctrl, p, z, p.nz, vv, red, a.role, true);
             __syncthreads();
         } else {
             // reductions (XY_REDUCE_FULL / XY_REDUCE_S)

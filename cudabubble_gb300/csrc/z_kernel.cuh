@@ -224,12 +224,28 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
     if (tid == 0) {
         bc[0] = (T)(ctrl->dt * p.ga);
         if constexpr (sizeof(T) == 4) {  // of the state the fused pass evaluated
-            if (a.mode <= Z_EULER) nonlin_lambdas<T>(p, ctrl, stage1 ? R_STATE : R_WORK, bc + 1);
+            if (a.mode <= Z_EULER) {
+                const int role = stage1 ? R_STATE : R_WORK;
+                nonlin_lambdas<T>(p, ctrl, role, bc + 1);
+                // N'(k = 0) whole, in FP64, from the fused pass's FP64 totals of G'' and
+                // w (or f): its terms (mean G'', the lambda1 constant, lambda2 f-hat(0))
+                // are ~1e2..1e3 and cancel to O(1), so summed in FP32 they move the
+                // volume by ~1e-4 of its step-to-step change, and E with it through the
+                // M1 penalty
+                const Scal& sc = ctrl->sc[role];
+                const bool euler = p.method == M_EULER;
+                const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
+                const double h0 = sc.sum_h * p.invN;
+                const double n0 = euler ? sc.sum_g * p.invN + 0.5 * lam1 + lam2 * h0
+                                        : sc.sum_g * p.invN - 0.5 * lam1 - 1.0606601717798212866 * lam2 * h0 * p.d_ieps;
+                bc[3] = (T)n0;
+            }
         }
     }
     __syncthreads();
     const T dtga = bc[0];
-    const T g_c = sizeof(T) == 4 ? bc[1] : (T)0, g_f = sizeof(T) == 4 ? bc[2] : (T)0;
+    const T g_f = sizeof(T) == 4 ? bc[2] : (T)0;  // bc[1], the lambda1 constant, enters n0
+    const T n0 = sizeof(T) == 4 ? bc[3] : (T)0;
     const bool ref4 = p.etd4_ref != 0;
     Acc<T> ag, ag2, al;
     static_assert(NT % TX == 0, "one column per thread");
@@ -267,6 +283,10 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
         const int kk_full = kxy + kzf * kzf;
         auto add_lam = [&](C& v, C xh) {
             if constexpr (sizeof(T) == 4) {
+                if (m == 0 && kz == 0) {  // the whole N'(0), formed in FP64 above
+                    v = cmk<C>(n0, (T)0);
+                    return;
+                }
                 C fh;
                 if (a.mode == Z_EULER) {
                     fh = wn;
@@ -277,7 +297,6 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                 }
                 v.x = fmaf(g_f, fh.x, v.x);
                 v.y = fmaf(g_f, fh.y, v.y);
-                if (m == 0 && kz == 0) v.x += g_c;
             }
             (void)xh;
         };
@@ -285,6 +304,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
         State<T> us;           // the new stage / state spectrum
         bool have_state = true;
         C un;
+        float2 dv = make_float2(0.f, 0.f);  // FP32 form: us - state, the transformed part of u
         if constexpr (sizeof(T) == 4) {
             // FP32 form: N-hat = N'-hat + c_lin u-hat (misc_kernels.cuh, lin_coef).  nh is
             // N'-hat; the c_lin terms act on the exact double-float spectra through the
@@ -302,16 +322,18 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                     }
                     us = sp.axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
                     us.store(ah, g);
+                    dv = us.diff(sp);
                     break;
                 }
                 case Z_ETD2_S2: {  // phi' = a (+) (c2 (N'_a - N'_u) + c2 c_lin d_a)
                     if constexpr (!g2) break;
                     const C nu = Nu[g];
-                    const State<T> sa = State<T>::load(ah, g);
+                    const State<T> sa = State<T>::load(ah, g), sp = State<T>::load(phat, g);
                     add_lam(nh, sa.work());
-                    const float2 da = sa.diff(State<T>::load(phat, g));
+                    const float2 da = sa.diff(sp);
                     us = sa.add(cmk<C>(fmaf(cf[3], da.x, cf[2] * (nh.x - nu.x)), fmaf(cf[3], da.y, cf[2] * (nh.y - nu.y))));
                     us.store(cand, g);
+                    dv = us.diff(sp);
                     break;
                 }
                 case Z_ETD4_S2:
@@ -329,6 +351,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                         add_lam(nh, sa.work());
                         Na[g] = nh;
                         us = sp.axpy(emh, inc_b(nh));
+                        dv = us.diff(sp);
                         break;
                     }
                     const C na = Na[g], nu = Nu[g];
@@ -344,6 +367,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                         add_lam(nh, cmk<C>(spw.x + db.x, spw.y + db.y));  // b = phi + d_b
                         Nb[g] = nh;
                         us = sa.axpy(emh, inc_c(nh));
+                        dv = us.diff(sp);
                         break;
                     }
                     // phi' = phi (+) (em'_4 phi + f1 N'_1 + f2 (N'_a + N'_b) + f3 N'_c
@@ -360,6 +384,7 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                         fmaf(cl, f1 * d1.y + f2 * (da.y + db.y) + f3 * dc.y, f1 * n1.y + f2 * (na.y + nb.y) + f3 * nh.y));
                     us = sp.axpy(cf[2], inc);
                     us.store(cand, g);
+                    dv = us.diff(sp);
                     break;
                 }
                 default: break;
@@ -421,14 +446,18 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
                     add_lam(nh, cmk<C>(0, 0));
                     Nu[g] = nh;
                 }
-                us = State<T>::load(phat, g).add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
+                const State<T> sp = State<T>::load(phat, g);
+                us = sp.add(cmk<C>(-dtga * nh.x, -dtga * nh.y));
                 us.store(cand, g);
+                if constexpr (sizeof(T) == 4) dv = us.diff(sp);
                 al.add(wxy * (nh.x * nh.x + nh.y * nh.y));
                 break;
             }
             case Z_INV_STATE: {
                 if constexpr (!gp) break;
                 us = State<T>::load(spec_of(I, ctrl, a.role), g);
+                if constexpr (sizeof(T) == 4)
+                    if (a.role != R_STATE) dv = us.diff(State<T>::load(phat, g));
                 break;
             }
             default: {  // Z_INV_PLAIN with an optional spectral multiplier
@@ -468,12 +497,16 @@ __global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ i
             // volume from the k = 0 mode: mean u = Re u-hat(0), exactly
             if (m == 0 && kz == 0) ctrl->sc[a.role].sum_u = us.re_exact() * (double)p.N;
         }
-        S[r * W + c] = un;
         if constexpr (sizeof(T) == 8) {
+            S[r * W + c] = un;
             const T mz = -cx * (T)(kzf * kzf);
             S[r * W + TX + c] = cmk<C>(mz * un.x, mz * un.y);
         } else {
-            const T kk = (T)(kzf * kzf);
+            // FP32 form (stepping modes and Z_INV_STATE): P0 carries u - u_state, which the
+            // fused xy pass adds to the state's double-float real-space field, and P2 the
+            // whole Laplacian -cx |k|^2 u-hat; plain modes keep u-hat and -cx kz^2 u-hat
+            S[r * W + c] = have_state ? cmk<C>(dv.x, dv.y) : un;
+            const T kk = (T)(have_state ? kzf * kzf + kxy : kzf * kzf);
             S[r * W + TX + c] = cmk<C>(-k.k_cx.mul(kk * un.x), -k.k_cx.mul(kk * un.y));
         }
     }

@@ -96,9 +96,7 @@ typedef struct cb_params {
                                 a plane's two fields do not fit one CTA (FP64 from 128^2, all 192^2+) */
     int pad0;
     double reject_tol;       /* adaptive loops reject an attempt when E_new > E_old + reject_tol |E_old|;
-                                < 0: default, 0 for CB_FP64 (the reference rule, belastic.cpp:653-668)
-                                and 1e-5 for CB_FP32, whose step-to-step energy changes carry up to
-                                ~5e-6 relative FP32 noise late in a relaxation */
+                                < 0: default 0, the reference rule (belastic.cpp:653-668), for both forms */
 } cb_params;
 
 typedef struct cb_scalars {

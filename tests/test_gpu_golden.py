@@ -4,11 +4,11 @@ through the C ABI.
 
 Bars: the plain FP64 form reproduces the reference to max|phi - phi_ref| <=
 1e-10 (fields to 1e-11 of their magnitude).  The FP32 form (FP32 FFT and
-pointwise, FP64 reductions) reaches a relative energy error <= 2e-6 along
-fixed-dt trajectories.  Its adaptive loops accept rises below reject_tol
-(1e-5 of E) that the reference would reject, so where the reference's
-accept/reject sequence turns on such a rise the two dt sequences part; those
-cases are held to the stated per-case bound and a matching rejection count.
+pointwise, FP64 reductions, the state's real-space field in double-float) is
+held to per-case relative energy bounds a few times above the measured
+errors, with the reference's rejection count.  Where an adaptive trajectory's
+accept / reject decision turns on a near-tie the dt sequences can part, and
+that case's bound says so.
 """
 import json
 import os
@@ -76,9 +76,12 @@ def test_fields_vs_reference(cblib, man, name, prec):
     st.close()
 
 
-# name, FP64 max|phi - phi_ref|, FP32 relative energy bound
-TRAJ = [("euler32", 1e-12, 2e-6), ("euler32_adapt", 1e-10, 1e-3), ("etd2_32", 1e-10, 2e-6),
-        ("etd2_48", 1e-10, 2e-6), ("c1_euler64", 1e-10, 2e-6)]
+# name, FP64 max|phi - phi_ref|, FP32 relative energy bound.  Measured FP32 errors on
+# GB300: euler32 3.6e-11, etd2_32 8.1e-9, etd2_48 2.7e-7, c1_euler64 2.0e-8;
+# euler32_adapt 2.9e-4 with the same 3 rejections (the Euler loop's dt sits at the
+# explicit stability limit and one accept / reject near-tie parts the dt sequences)
+TRAJ = [("euler32", 1e-12, 1e-9), ("euler32_adapt", 1e-10, 1e-3), ("etd2_32", 1e-10, 1e-7),
+        ("etd2_48", 1e-10, 1e-6), ("c1_euler64", 1e-10, 1e-7)]
 
 
 @pytest.mark.parametrize("prec", [0, 1], ids=["fp64", "fp32"])
@@ -110,13 +113,12 @@ def test_trajectory_vs_reference(cblib, man, name, tol64, relE32, prec):
 
 def test_config2_fp32_energy_error_vs_reference(cblib, man):
     """Workload config 2: 128^3 ETD-RK2, adaptive dt from 1e-6, 1000 steps,
-    against the reference's FP64 cuFFT trajectory.  Measured on GB300: the
-    FP32 form tracks the reference's accept/reject sequence exactly for the
-    first ~380 steps with relative energy error ~1e-7..4e-6 (the FP32
-    transform noise floor); later near-tie rejections can part the dt
-    sequences, and at step 1000 the error is ~4e-6..1e-5 with the same
-    rejection count.  Bars: 5e-6 through step 300, 3e-5 at 1000, rejection
-    count within 5."""
+    against the reference's FP64 cuFFT trajectory.  The FP32 form makes the
+    reference's accept / reject decisions step for step under its strict rule
+    (248 rejections, all on the same steps).  Measured on GB300: relative
+    energy error <= 9.8e-7 at every checkpoint (largest at steps 10..30, where
+    dt = 8e-6 stresses the volume penalty) and 7e-9 at step 1000.  Bar: the
+    the benchmark spec's 1e-6 at every checkpoint, rejections equal throughout."""
     from cudabubble_gb300 import capi, shapes
     case = man["cases"]["c2_etd2_128"]
     phi0 = shapes.seeded_ellipsoid(128, 128, shapes.eps_rule(150, 128), 2)
@@ -124,15 +126,11 @@ def test_config2_fp32_energy_error_vs_reference(cblib, man):
     st.set_phi(phi0)
     ref = {s["step"]: s for s in case["steps"]}
     errs = {}
-    for k in (1, 10, 100, 300, 1000):
+    for k in (1, 10, 20, 30, 100, 150, 300, 500, 700, 1000):
         st.run(k - st.scalars()["steps"])
         s = st.scalars()
         errs[k] = abs(s["E"] - ref[k]["E"]) / abs(ref[k]["E"])
-        if k <= 300:
-            assert s["rejects"] == ref[k]["rejects"], (k, s["rejects"], ref[k]["rejects"])
-    print("config 2 FP32 rel E error vs reference:", {k: f"{v:.2e}" for k, v in errs.items()},
-          "rejects", s["rejects"], "reference", ref[1000]["rejects"])
-    assert max(errs[k] for k in (1, 10, 100, 300)) <= 5e-6, errs
-    assert errs[1000] <= 3e-5, errs
-    assert abs(s["rejects"] - ref[1000]["rejects"]) <= 5
+        assert s["rejects"] == ref[k]["rejects"], (k, s["rejects"], ref[k]["rejects"])
+    print("config 2 FP32 rel E error vs reference:", {k: f"{v:.2e}" for k, v in errs.items()})
+    assert max(errs.values()) <= 1e-6, errs
     st.close()
