@@ -18,6 +18,7 @@ template <> struct Acc<double> {
 template <> struct Acc<float> {
     FF v{0.f, 0.f};
     __device__ __forceinline__ void add(float x) { v = ff_add(v, FF{x, 0.f}); }
+    __device__ __forceinline__ void add(float x, float xlo) { v = ff_add(v, FF{x, xlo}); }  // x + xlo
     __device__ __forceinline__ FF part() const { return v; }
 };
 
@@ -125,20 +126,31 @@ __device__ __forceinline__ float2 ff_add_f(float2 U, float v) {
     return make_float2(hi, e - (hi - s));
 }
 
-// XY_FUSED point of the FP32 form from u = uh + ul.  u^2 - 1 is formed as
-// (uh - s)(uh + s) + 2 uh ul with s = +-1: uh - s is exact where |uh| is within a
-// factor 2 of 1, so u^2 - 1 and w = (u^2 - 1) u keep their relative accuracy where
-// u = +-1 + d with d far below FP32's spacing at 1; elsewhere u^2 - 1 is O(1) and
-// plain FP32 rounding is enough.  Otherwise as fused_point<float>.
+// XY_FUSED point of the FP32 form from u = uh + ul.  u^2 - 1 is formed as an
+// unevaluated pair: uh^2 = p + pe exactly (TwoProd), p - 1 = s + se exactly
+// (TwoSum), plus pe, se and 2 uh ul, so u^2 - 1 and w = (u^2 - 1) u keep their
+// relative accuracy where u = +-1 + d with d far below FP32's spacing at 1.  Its
+// square is summed to the same accuracy: that sum carries S, whose error moves
+// the area penalty's lambda2 and, through it, the volume (a plain FP32 u^2 - 1
+// put ~1e-8 into S).  __fmul_rn / __fadd_rn keep nvcc from contracting the
+// error-free steps into FMAs.  Otherwise as fused_point<float>.
 __device__ __forceinline__ void fused_point_u(const PC<float>& k, bool euler, float uh, float ul, float lap,
                                               Acc<float>& as, Acc<float>& af, float& g, float& h) {
     const float D = 1.5f;
-    const float sg = uh < 0.f ? -1.f : 1.f;
-    const float u2m = fmaf(uh - sg, uh + sg, 2.f * uh * ul);
+    const float p = __fmul_rn(uh, uh);
+    const float pe = fmaf(uh, uh, -p);
+    const float s = __fadd_rn(p, -1.f);
+    const float sb = __fadd_rn(s, -p);
+    const float se = __fadd_rn(__fadd_rn(p, -__fadd_rn(s, -sb)), __fadd_rn(-1.f, -sb));
+    const float t = se + pe + 2.f * uh * ul;
+    const float u2m = __fadd_rn(s, t);
+    const float tb = __fadd_rn(u2m, -s);
+    const float u2m_lo = __fadd_rn(__fadd_rn(s, -__fadd_rn(u2m, -tb)), __fadd_rn(t, -tb));
+    const float sq = __fmul_rn(u2m, u2m);
     const float u2 = u2m + 1.f;
     const float w = u2m * uh;
     const float f = k.k_ieps.mul(w) - k.k_eps.mul(lap);
-    as.add(u2m * u2m);
+    as.add(sq, fmaf(u2m, u2m, -sq) + 2.f * u2m * u2m_lo);
     af.add(f * f);
     if (euler) {
         g = k.k_K2.mul((3.f * u2 - 1.f) * f);

@@ -101,12 +101,16 @@ template <> struct State<float> {
         return make_float2((hi.x - o.hi.x) + (lo.x - o.lo.x), (hi.y - o.hi.y) + (lo.y - o.lo.y));
     }
     // w |u|^2 with u = hi + lo: hi^2 exactly via FMA, the rest in a second sum
+    // (w up to 3 (n/2)^2 times an exact square needs more than 24 bits: each product
+    // is split error-free, or its rounding, ~6e-8 of the term, reaches S at ~1e-9 and
+    // the area penalty's lambda2 with it)
     template <class A> __device__ __forceinline__ void norm2_into(A& big, A& small, float w) const {
         const float px = hi.x * hi.x, py = hi.y * hi.y;
         const float ex = fmaf(hi.x, hi.x, -px), ey = fmaf(hi.y, hi.y, -py);
-        big.add(w * px);
-        big.add(w * py);
-        small.add(w * (ex + ey + 2.f * (hi.x * lo.x + hi.y * lo.y)));
+        const float wx = w * px, wy = w * py;
+        big.add(wx);
+        big.add(wy);
+        small.add(fmaf(w, px, -wx) + fmaf(w, py, -wy) + w * (ex + ey + 2.f * (hi.x * lo.x + hi.y * lo.y)));
     }
 };
 
