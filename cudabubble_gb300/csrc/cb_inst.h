@@ -142,8 +142,9 @@ template <class T> struct InstT {
     void* B;
     void* Y[2];       // split plane path: y-transformed fields (nullptr when unused)
     void* G[2][2];    // FP32 form: XY_FUSED outputs (G'', w) of the state / candidate (ctrl->ab_state)
-    // FP32 form: real-space u of the state / candidate as double-float pairs
-    // [z][y][x] (ctrl->u_state).  The z pass transforms only u - u_state, and the
+    // FP32 form: real-space u of the state / candidate as double-float pairs, rows
+    // [z][y] of nx/2 float4 (two points each) in the fused passes' x-slot order
+    // (ctrl->u_state).  The z pass transforms only u - u_state, and the
     // fused pass adds it to U[u_state]: u from a plain FP32 transform carries
     // ~6e-8 absolute error, which where u = +-1 + d with d below it makes
     // w = u^3 - u ~ +-2 d wrong by 100 %, with one sign over the whole far field

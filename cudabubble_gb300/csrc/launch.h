@@ -32,7 +32,8 @@ template <class T> struct Launch {
 
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,
                              const double* d, double eps, double x0, double x1, double x2, cudaStream_t s);
-// real FP64 field -> double-float pairs (hi = fl32(v), lo = fl32(v - hi)), n points
-cudaError_t launch_real_to_ff(const double* in, void* out, size_t n, cudaStream_t s);
+// real FP64 field of nrows rows of nx points -> double-float pairs (hi = fl32(v),
+// lo = fl32(v - hi)), two points per float4 in the fused passes' x-slot order
+cudaError_t launch_real_to_ff(const double* in, void* out, size_t nrows, int nx, cudaStream_t s);
 
 }  // namespace cb

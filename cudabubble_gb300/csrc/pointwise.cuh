@@ -22,6 +22,21 @@ template <> struct Acc<float> {
     __device__ __forceinline__ FF part() const { return v; }
 };
 
+// A plain per-thread sum, handed to the same double-float / FP64 warp and block
+// reductions as Acc: for totals that tolerate one FP32 rounding per add (the
+// fused pass's totals of G'' and w, whose FP64 N'(0) needs ~1e-6 absolute)
+template <class T> struct PSum;
+template <> struct PSum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double part() const { return s; }
+};
+template <> struct PSum<float> {
+    float s = 0.f;
+    __device__ __forceinline__ void add(float x) { s += x; }
+    __device__ __forceinline__ FF part() const { return FF{s, 0.f}; }
+};
+
 // lambda_1 = M1 (V - alpha), lambda_2 = M2 (S - beta) (belastic.cpp:478-479) as
 // the constant and f coefficients of G, formed in FP64 by one thread.
 template <class T> __device__ __forceinline__ void nonlin_lambdas(const Params& p, const Ctrl* ctrl, int role, T* lam) {

@@ -241,14 +241,15 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
             __syncthreads();
         } else if (a.mode == XY_FUSED) {
             const bool euler = p.method == M_EULER;
-            Acc<T> as, af, ag, ah;
+            Acc<T> as, af;
+            PSum<T> ag, ah;
             if constexpr (sizeof(T) == 4) {
                 // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
                 const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + row0 * M;
                 float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + row0 * M : nullptr;
                 for (int it = tid; it < RPC * M; it += NT) {
                     const int q = it % M, j = it / M;
-                    const int ui = j * M + tidx<M>(q);  // row j, points 2m and 2m + 1
+                    const int ui = j * M + q;  // row j, x slot q (the field is stored in x-slot order)
                     const float4 Uv = __ldg(Us + ui);
                     C* pu = S + j * LP + q;
                     C* pl = S + (RPC + j) * LP + q;

@@ -497,7 +497,7 @@ template <class T> class Stepper final : public Handle {
         reset_ctrl();
         CB_CK(push());
         // FP32 form: the state's real-space field, exact as a double-float pair
-        if (sizeof(T) == 4) CB_CK(launch_real_to_ff(src, h.U[0], (size_t)p.N, st));
+        if (sizeof(T) == 4) CB_CK(launch_real_to_ff(src, h.U[0], (size_t)p.nz * p.ny, p.nx, st));
         if (aux) {  // exact spectrum: FP64 transform into the 16 B/mode candidate field, then hi/lo split
             CB_CK(fwd3d_f64(src, h.spec[1], h.ahat));
             CB_CK(Launch<T>::f64_to_state(h.spec[1], h.spec[0], ns, 1, st));

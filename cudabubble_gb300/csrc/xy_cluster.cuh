@@ -150,14 +150,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     // ---- sums and lambda-free partials G'', w of this CTA's rows
     {
         const bool euler = p.method == M_EULER;
-        Acc<T> as, af, ag, ah;
+        Acc<T> as, af;
+        PSum<T> ag, ah;
         // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
         const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
         float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
                                       : nullptr;
         for (int it = tid; it < NH * M; it += NT) {
             const int qq = it % M, r = it / M;
-            const int ui = tidx<NY>(rank * NH + r) * M + tidx<M>(qq);  // row y, points 2m and 2m + 1
+            const int ui = tidx<NY>(rank * NH + r) * M + qq;  // row y, x slot qq (stored in x-slot order)
             const float4 Uv = __ldg(Us + ui);
             C* pu = S + r * PX + qq;
             C* pl = pu + M;

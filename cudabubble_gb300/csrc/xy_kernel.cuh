@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         } else if (a.mode == XY_FUSED) {
             // sums of the state and its lambda-free partials G'', w in one sweep
             const bool euler = p.method == M_EULER;
-            Acc<T> as, af, ag, ah;
+            Acc<T> as, af;
+            PSum<T> ag, ah;
             if constexpr (sizeof(T) == 4) {
                 // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
                 const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                                               : nullptr;
                 for (int it = tid; it < NY * M; it += NT) {
                     const int q = it % M, r = it / M;
-                    const int ui = tidx<NY>(r) * M + tidx<M>(q);  // row y, points 2m and 2m + 1
+                    const int ui = tidx<NY>(r) * M + q;  // row y, x slot q (stored in x-slot order)
                     const float4 Uv = __ldg(Us + ui);
                     C* pu = S + r * pitch + q;
                     C* pl = pu + M;
