@@ -37,7 +37,7 @@ class cb_params(C.Structure):
                 ("precision", C.c_int), ("grow_every", C.c_int), ("grow_factor", C.c_double),
                 ("dt_cap", C.c_double), ("cap_probe", C.c_double), ("etd4_textbook", C.c_int),
                 ("accurate_coefficients", C.c_int), ("rel_tol", C.c_double), ("xy_split", C.c_int),
-                ("pad0", C.c_int), ("reject_tol", C.c_double)]
+                ("pad0", C.c_int), ("reject_tol", C.c_double), ("spont_c", C.c_double)]
 
 
 class cb_scalars(C.Structure):

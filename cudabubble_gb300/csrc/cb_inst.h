@@ -93,6 +93,7 @@ struct Params {
     double tmax;        // Euler loop time limit (belastic.cpp:407)
     double rel_tol;     // > 0: stop once an accepted step changes E by < rel_tol |E|
     double reject_tol;  // adaptive: reject when E_new > E_old + reject_tol |E_old|
+    double C;           // spontaneous curvature (plain FP64 form; 0 in the reference)
     // host-precomputed constants: GB300 runs FP64 at a small fraction of its
     // FP32 rate, so kernels read these instead of dividing per thread
     double d_ieps, d_ieps2, d_ieps3, d_bnl;  // 1/eps, 1/eps^2, 1/eps^3, beta * cx
@@ -116,11 +117,11 @@ template <> struct PC<float> {
           k_invN{p.fk[FK_INVN][0], p.fk[FK_INVN][1]}, k_cx{p.fk[FK_CX][0], p.fk[FK_CX][1]} {}
 };
 template <> struct PC<double> {
-    double eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    double eps, ieps, ieps2, ieps3, bnl, cx, invN, eta, C;
     KC<double> k_eps, k_ieps, k_K2, k_K3, k_bnl, k_invN, k_cx;
     __device__ __forceinline__ explicit PC(const Params& p)
         : eps(p.eps), ieps(p.d_ieps), ieps2(p.d_ieps2), ieps3(p.d_ieps3), bnl(p.d_bnl), cx(p.cx), invN(p.invN),
-          eta(p.eta), k_eps{p.eps}, k_ieps{p.d_ieps}, k_K2{p.eta * p.d_ieps2}, k_K3{p.eta * 1.5 * p.d_ieps3},
+          eta(p.eta), C(p.C), k_eps{p.eps}, k_ieps{p.d_ieps}, k_K2{p.eta * p.d_ieps2}, k_K3{p.eta * 1.5 * p.d_ieps3},
           k_bnl{p.d_bnl}, k_invN{p.invN}, k_cx{p.cx} {}
 };
 

@@ -61,12 +61,26 @@ __device__ __forceinline__ void nonlin_point(const PC<T>& k, bool euler, T g_c, 
     if constexpr (sizeof(T) == 8) {
         const T f = -lap * k.eps + (u2 - (T)1) * u * k.ieps;
         if (euler) {
-            g = g_c + g_f * f + k.eta * ((T)3 * u2 - (T)1) * f * k.ieps2;
-            h = f;
+            if (k.C != 0.0) {  // g = -lap fc + (3u^2 - 1 + 2 eps u C) fc / eps^2 (phasefield.cpp:236-246)
+                const T fc = f + (u2 - (T)1) * k.C;
+                g = g_c + g_f * f + k.eta * ((T)3 * u2 - (T)1 + (T)2 * k.eps * u * k.C) * fc * k.ieps2;
+                h = fc;
+            } else {
+                g = g_c + g_f * f + k.eta * ((T)3 * u2 - (T)1) * f * k.ieps2;
+                h = f;
+            }
         } else {
             const T t = u * (u2 - (T)1 - kappa);
             g = g_c + g_f * f - k.eta * (D * t * k.ieps3 + ((T)3 * u2 - D - (T)1) * k.ieps2 * f);
             h = t;
+            if (k.C != 0.0) {
+                // no counterpart in the reference (its nld ignores C): the curvature part
+                // g_C - g0 = -lap (C (u^2 - 1)) + ((3u^2 - 1)(fc - f) + 2 eps u C fc) / eps^2
+                // whole in the nonlinear term; its Laplacian rides on H (eta lap t / eps)
+                const T cu = (u2 - (T)1) * k.C, fc = f + cu;
+                g -= k.eta * (((T)3 * u2 - (T)1) * cu + (T)2 * k.eps * u * k.C * fc) * k.ieps2;
+                h = t + k.eps * cu;
+            }
         }
     } else {
         const T w = (u2 - (T)1) * u;
@@ -93,7 +107,7 @@ __device__ __forceinline__ void reduce_point(const PC<T>& k, bool full, T u, T l
     as.add(u2m * u2m);
     if (full) {
         T f;
-        if constexpr (sizeof(T) == 8) f = -lap * k.eps + u2m * u * k.ieps;
+        if constexpr (sizeof(T) == 8) f = -lap * k.eps + u2m * u * k.ieps + u2m * k.C;  // fc (phasefield.cpp:318-325)
         else f = k.k_ieps.mul(u2m * u) - k.k_eps.mul(lap);
         af.add(f * f);
     }

@@ -129,6 +129,9 @@ inline int make_params(const cb_params& u, Eff& e) {
         return fail(CB_EINVAL, "grid %dx%dx%d: nx must be even and positive (Calc.cu:52-55)", u.nx, u.nx, u.nz);
     if (u.method < CB_EULER || u.method > CB_ETD4) return fail(CB_EINVAL, "unknown method %d", u.method);
     if (u.precision != CB_FP64 && u.precision != CB_FP32) return fail(CB_EINVAL, "unknown precision %d", u.precision);
+    if (u.spont_c != 0.0 && u.precision != CB_FP64)
+        return fail(CB_EUNSUPPORTED, "spontaneous curvature runs in the plain FP64 form (precision CB_FP64)");
+    if (!std::isfinite(u.spont_c)) return fail(CB_EINVAL, "spontaneous curvature must be finite");
     p.nx = u.nx;
     p.ny = u.nx;  // Calc.cu:45-46
     p.nz = u.nz;
@@ -160,6 +163,7 @@ inline int make_params(const cb_params& u, Eff& e) {
     // both forms default to the reference's strict E_new > E_old rejection
     // (belastic.cpp:653-668); a positive reject_tol tolerates rises below reject_tol |E|
     p.reject_tol = u.reject_tol >= 0 ? u.reject_tol : 0.0;
+    p.C = u.spont_c;
     // nonlinear term N-hat = A-hat + beta cx |k|^2 B-hat: beta = eta (Euler, -lap f in g0)
     // or -eta/eps (ETD, +lap t / eps in -eta NL)
     const double beta = euler ? p.eta : -p.eta / p.eps;

@@ -97,6 +97,9 @@ typedef struct cb_params {
     int pad0;
     double reject_tol;       /* adaptive loops reject an attempt when E_new > E_old + reject_tol |E_old|;
                                 < 0: default 0, the reference rule (belastic.cpp:653-668), for both forms */
+    double spont_c;          /* spontaneous curvature C of fc = f + (phi^2 - 1) C, from the reference's
+                                commented-out formulas (phasefield.cpp:183-250); 0 (the reference, whose
+                                curvature field is NULL, fluidbase.cpp:150) or, in CB_FP64 only, any value */
 } cb_params;
 
 typedef struct cb_scalars {

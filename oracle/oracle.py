@@ -189,9 +189,10 @@ class PhaseField:
     (``phasefield.cpp:14-332``).  ``update_d``/``update_fd`` invalidate every
     cache exactly like ``phasefield.cpp:95-123``."""
 
-    def __init__(self, calc: Calc, eps: float, d: np.ndarray | None = None):
+    def __init__(self, calc: Calc, eps: float, d: np.ndarray | None = None, C: float = 0.0):
         self.calc = calc
         self.eps = eps
+        self.C = C  # spontaneous curvature; the reference's m_C is always NULL (fluidbase.cpp:150)
         self.d = np.zeros(calc.shape) if d is None else np.array(d, dtype=np.float64)
         self._c = {}
 
@@ -216,8 +217,27 @@ class PhaseField:
     def f(self):  # phasefield.cpp:173-181
         return self._get("f", lambda: self.calc.f(self.lap(), self.d, self.eps))
 
-    def g0(self):  # phasefield.cpp:205-221 (g() == g0() since C == NULL, :223-225)
+    def g0(self):  # phasefield.cpp:205-221
         return self._get("g0", lambda: self.calc.g0(self.calc.lap(self.f()), self.d, self.f(), self.eps))
+
+    def fc(self):
+        """phasefield.cpp:183-203: f itself without a curvature field (:185); with a
+        constant C the commented-out loop's fc = f + (phi^2 - 1) C (:192-198)."""
+        if self.C == 0.0:
+            return self.f()
+        return self._get("fc", lambda: self.f() + (self.d * self.d - 1.0) * self.C)
+
+    def g(self):
+        """phasefield.cpp:223-250: g0 without a curvature field (:225); with C the
+        commented-out loop's g = -lap fc + (3 phi^2 - 1 + 2 eps phi C) fc / eps^2
+        (:236-246)."""
+        if self.C == 0.0:
+            return self.g0()
+        def mk():
+            fc = self.fc()
+            e = self.eps
+            return -self.calc.lap(fc) + (3.0 * self.d * self.d - 1.0 + 2.0 * e * self.d * self.C) * fc / (e * e)
+        return self._get("g", mk)
 
     def nld(self):  # phasefield.cpp:253-267
         return self._get("nld", lambda: self.calc.nld(self.d, self.f(), self.eps))
@@ -237,8 +257,8 @@ class PhaseField:
     def surface(self):  # phasefield.cpp:310-316
         return self._get("surf", lambda: self.calc.intf(self.s(), 0.0, SURF_C))
 
-    def elastic_eng(self):  # phasefield.cpp:318-325 (fc() == f() since C == NULL)
-        return self._get("eel", lambda: self.calc.intf(self.f() * self.f(), 0.0, 1.0 / (self.eps * 2.0)))
+    def elastic_eng(self):  # phasefield.cpp:318-325 (of fc)
+        return self._get("eel", lambda: self.calc.intf(self.fc() * self.fc(), 0.0, 1.0 / (self.eps * 2.0)))
 
     def LSerror(self, u):  # phasefield.cpp:327-332
         return self.calc.intf(u * u, 0.0, 1.0)
@@ -267,6 +287,7 @@ class Params:
     time_step: float = 1e-6
     fixed_time_step: float = 0.0
     b_shape: int = 0
+    C: float = 0.0  # spontaneous curvature (not in the reference, which keeps m_C NULL)
     # adaptive-dt schedule (belastic.cpp:644-651 for ETD, :376-378 for Euler)
     grow_every: int = 4
     grow_factor: float = 2.0
@@ -323,8 +344,8 @@ class Belastic:
         if self.beta < 0:  # fluidbase.cpp:143
             self.alpha = self.beta = 0.0
         self.time_step = p.time_step
-        self.pd = PhaseField(self.calc, self.eps, phi0)  # belastic.cpp:19
-        self.pa = PhaseField(self.calc, self.eps)  # belastic.cpp:20
+        self.pd = PhaseField(self.calc, self.eps, phi0, p.C)  # belastic.cpp:19
+        self.pa = PhaseField(self.calc, self.eps, None, p.C)  # belastic.cpp:20
         self.Het = None
         self.steps = 0
         self.rejects = 0
@@ -336,11 +357,11 @@ class Belastic:
             self.alpha = self.pd.vol()
             self.beta = self.pd.surface()
 
-    # belastic.cpp:52-64
+    # belastic.cpp:52-64 (pd->g(), which is g0 without a curvature field)
     def get_sum_fgqterm(self, pd: PhaseField) -> np.ndarray:
         lamb1 = self.p.M1 * (pd.vol() - self.alpha)
         lamb2 = self.p.M2 * (pd.surface() - self.beta)
-        return self.calc.nld1(pd.f(), pd.g0(), lamb1, lamb2, self.p.eta)
+        return self.calc.nld1(pd.f(), pd.g(), lamb1, lamb2, self.p.eta)
 
     # belastic.cpp:68-86
     def getstaticenergy(self, pd: PhaseField, constrained: bool = True) -> float:
@@ -355,7 +376,13 @@ class Belastic:
     def get_nld_term(self, pd: PhaseField) -> np.ndarray:
         lamb1 = self.p.M1 * (pd.vol() - self.alpha)
         lamb2 = self.p.M2 * (pd.surface() - self.beta)
-        tmp = self.calc.nld2(pd.f(), pd.nld(), lamb1, lamb2, self.p.eta)
+        nld = pd.nld()
+        if pd.C != 0.0:
+            # no counterpart in the reference, whose nld ignores C: the curvature terms
+            # g - g0 enter the nonlinear part whole, so that with the linear part L the
+            # ETD right-hand side is the Euler loop's -eta g again (nld = g0 + L phi)
+            nld = nld + (pd.g() - pd.g0())
+        tmp = self.calc.nld2(pd.f(), nld, lamb1, lamb2, self.p.eta)
         return self.calc.r2c_3d_f(tmp)
 
     def init_fEIF(self):  # belastic.cpp:614

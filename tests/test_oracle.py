@@ -238,3 +238,32 @@ def test_oracle_shape_adjust_matches_reference(name, phi_tol, e_tol):
     err = np.abs(b.pd.d - g["phi_adjust"]).max()
     assert err < phi_tol, err
     assert b.getstaticenergy(b.pd, False) == pytest.approx(case["scalars"]["E"], rel=e_tol)
+
+
+@pytest.mark.parametrize("C", [0.8, -0.5])
+def test_curvature_g_is_the_variational_derivative(C):
+    """Spontaneous curvature, restated from the reference's commented-out loops
+    (phasefield.cpp:183-250), which never ran (its curvature field is NULL,
+    fluidbase.cpp:150): g_C = -lap fc + (3 phi^2 - 1 + 2 eps phi C) fc / eps^2 is
+    the variational derivative of E_el = int fc^2 / (2 eps), fc = f + (phi^2 - 1) C.
+    Central differences of the oracle's E_el along a smooth direction match
+    <g_C, delta> dV to their own truncation error."""
+    n = 24
+    eps = O.eps_from_epssize(200, 2 * math.pi, n)
+    calc = O.Calc(n, n, 2 * math.pi)
+    phi = O.ellipsoid_phi0(n, n, eps, (1.6, 1.4, 1.0))
+    x = O.grid_coords(n, 2 * math.pi)
+    # a smooth direction with no parity shared with the centred ellipsoid
+    delta = (np.cos(x + 0.4)[None, None, :] * np.cos(2 * x + 0.1)[None, :, None] * np.cos(x + 0.3)[:, None, None])
+    pd = O.PhaseField(calc, eps, phi, C)
+    g = pd.g()
+    dV = (2 * math.pi) ** 3 / calc.N
+    lin = float(np.sum(g * delta)) * dV
+    assert abs(lin) > 1e-2
+    h = 1e-5
+    Ep = O.PhaseField(calc, eps, phi + h * delta, C).elastic_eng()
+    Em = O.PhaseField(calc, eps, phi - h * delta, C).elastic_eng()
+    assert (Ep - Em) / (2 * h) == pytest.approx(lin, rel=1e-6)
+    # and C = 0 is the reference's own path, bit for bit
+    p0 = O.PhaseField(calc, eps, phi, 0.0)
+    assert np.array_equal(p0.g(), p0.g0()) and p0.elastic_eng() == O.PhaseField(calc, eps, phi).elastic_eng()
