@@ -33,6 +33,14 @@ template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, 
 template <class C, class T> __device__ __forceinline__ C cscale(C a, T s) { return cmk<C>(a.x * s, a.y * s); }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, class C> __device__ __forceinline__ C cmul_mi(C a) { return INV ? cmk<C>(-a.y, a.x) : cmk<C>(a.y, -a.x); }
+// FP32 complex add / subtract as one packed instruction (FADD2, sm_100 and later):
+// the same two IEEE round-to-nearest additions in one issue slot
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+#endif
 
 // ------------------------------------------------- compile-time twiddles
 // cos(pi * a / b) for b in {6, 8}: the only angles the radix <= 16 codelets
@@ -85,6 +93,8 @@ template <bool INV, class C> __device__ __forceinline__ C tw_get_pre(C w) { retu
 // so the only errors left are unbiased roundings.  The FP64 form keeps plain
 // products.
 __device__ __forceinline__ float2 cmul_comp(float2 a, float c, float s, float cl, float sl) {
+    // (packed FFMA2 / FMUL2 forms need the operand broadcasts (a.x, a.x), (a.y, a.y) and
+    // lane swaps of the twiddle; measured on GB300 they cost what they save)
     const float rx = fmaf(a.x, c, fmaf(-a.y, s, fmaf(-a.y, sl, a.x * cl)));
     const float ry = fmaf(a.x, s, fmaf(a.y, c, fmaf(a.y, cl, a.x * sl)));
     return make_float2(rx, ry);
