@@ -145,47 +145,95 @@ __device__ __forceinline__ void fused_point(const PC<T>& k, bool euler, T u, T l
     }
 }
 
-// FP32 form: u = U + v as a double-float pair, U = (hi, lo) the state's real-space
-// field and v the FP32 transform of u - u_state (TwoSum, then FastTwoSum)
-__device__ __forceinline__ float2 ff_add_f(float2 U, float v) {
-    const float s = U.x + v;
-    const float bp = s - U.x;
-    const float e = ((U.x - (s - bp)) + (v - bp)) + U.y;
-    const float hi = s + e;
-    return make_float2(hi, e - (hi - s));
+// ---- two real points per complex slot, two FP32 lanes per instruction
+// The fused passes hold real values two to a complex slot (x = 2m, 2m + 1), and
+// every pointwise step treats the two alike, so they run as lane-wise float2
+// arithmetic: packed FADD2 / FMUL2 / FFMA2 on sm_100 and later, the same IEEE
+// round-to-nearest operations per lane (explicit, so never contracted).
+namespace lane2 {
+__device__ __forceinline__ float2 bc(float v) { return make_float2(v, v); }
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+#else
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) {
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
+#endif
+__device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return add(a, neg(b)); }
+// x * k with k = hi + lo folded before the rounding (KC<float>::mul per lane)
+__device__ __forceinline__ float2 kmul(const KC<float>& k, float2 x) { return fma(x, bc(k.hi), mul(x, bc(k.lo))); }
+}  // namespace lane2
+
+// two lanes of Acc<float> (per-lane TwoSum + FastTwoSum, as ff_add), joined at the end
+struct Acc2 {
+    float2 hi{0.f, 0.f}, lo{0.f, 0.f};
+    __device__ __forceinline__ void add(float2 x, float2 xl) {
+        using namespace lane2;
+        const float2 s = lane2::add(hi, x);
+        const float2 bp = sub(s, hi);
+        const float2 e = lane2::add(lane2::add(sub(hi, sub(s, bp)), sub(x, bp)), lane2::add(lo, xl));
+        hi = lane2::add(s, e);
+        lo = sub(e, sub(hi, s));
+    }
+    __device__ __forceinline__ FF part() const { return ff_add(FF{hi.x, lo.x}, FF{hi.y, lo.y}); }
+};
+// two lanes of PSum<float>
+struct PSum2 {
+    float2 s{0.f, 0.f};
+    __device__ __forceinline__ void add(float2 x) { s = lane2::add(s, x); }
+    __device__ __forceinline__ FF part() const { return ff_add(FF{s.x, 0.f}, FF{s.y, 0.f}); }
+};
+
+// u = U + v for the two points of a slot as double-float pairs (TwoSum, then
+// FastTwoSum, per lane): U = (hi0, lo0, hi1, lo1) the state's real-space field,
+// v the FP32 transform of u - u_state
+__device__ __forceinline__ void ff_add_f2(float4 U, float2 v, float2& uh, float2& ul) {
+    using namespace lane2;
+    const float2 Uh = make_float2(U.x, U.z), Ul = make_float2(U.y, U.w);
+    const float2 s = lane2::add(Uh, v);
+    const float2 bp = sub(s, Uh);
+    const float2 e = lane2::add(lane2::add(sub(Uh, sub(s, bp)), sub(v, bp)), Ul);
+    uh = lane2::add(s, e);
+    ul = sub(e, sub(uh, s));
 }
 
-// XY_FUSED point of the FP32 form from u = uh + ul.  u^2 - 1 is formed as an
-// unevaluated pair: uh^2 = p + pe exactly (TwoProd), p - 1 = s + se exactly
-// (TwoSum), plus pe, se and 2 uh ul, so u^2 - 1 and w = (u^2 - 1) u keep their
-// relative accuracy where u = +-1 + d with d far below FP32's spacing at 1.  Its
-// square is summed to the same accuracy: that sum carries S, whose error moves
-// the area penalty's lambda2 and, through it, the volume (a plain FP32 u^2 - 1
-// put ~1e-8 into S).  __fmul_rn / __fadd_rn keep nvcc from contracting the
-// error-free steps into FMAs.  Otherwise as fused_point<float>.
-__device__ __forceinline__ void fused_point_u(const PC<float>& k, bool euler, float uh, float ul, float lap,
-                                              Acc<float>& as, Acc<float>& af, float& g, float& h) {
-    const float D = 1.5f;
-    const float p = __fmul_rn(uh, uh);
-    const float pe = fmaf(uh, uh, -p);
-    const float s = __fadd_rn(p, -1.f);
-    const float sb = __fadd_rn(s, -p);
-    const float se = __fadd_rn(__fadd_rn(p, -__fadd_rn(s, -sb)), __fadd_rn(-1.f, -sb));
-    const float t = se + pe + 2.f * uh * ul;
-    const float u2m = __fadd_rn(s, t);
-    const float tb = __fadd_rn(u2m, -s);
-    const float u2m_lo = __fadd_rn(__fadd_rn(s, -__fadd_rn(u2m, -tb)), __fadd_rn(t, -tb));
-    const float sq = __fmul_rn(u2m, u2m);
-    const float u2 = u2m + 1.f;
-    const float w = u2m * uh;
-    const float f = k.k_ieps.mul(w) - k.k_eps.mul(lap);
-    as.add(sq, fmaf(u2m, u2m, -sq) + 2.f * u2m * u2m_lo);
-    af.add(f * f);
+// XY_FUSED points of the FP32 form (two per slot, lane-wise) from u = uh + ul.
+// u^2 - 1 is formed as an unevaluated pair: uh^2 = p + pe exactly (TwoProd),
+// p - 1 = s + se exactly (TwoSum), plus pe, se and 2 uh ul, so u^2 - 1 and
+// w = (u^2 - 1) u keep their relative accuracy where u = +-1 + d with d far
+// below FP32's spacing at 1.  Its square is summed to the same accuracy: that
+// sum carries S, whose error moves the area penalty's lambda2 and, through it,
+// the volume (a plain FP32 u^2 - 1 put ~1e-8 into S).  Otherwise as
+// fused_point<float>.
+__device__ __forceinline__ void fused_point_u2(const PC<float>& k, bool euler, float2 uh, float2 ul, float2 lap,
+                                               Acc2& as, Acc2& af, float2& g, float2& h) {
+    using namespace lane2;
+    const float2 one = bc(1.f), mone = bc(-1.f);
+    const float2 p = mul(uh, uh);
+    const float2 pe = fma(uh, uh, neg(p));
+    const float2 s = lane2::add(p, mone);
+    const float2 sb = sub(s, p);
+    const float2 se = lane2::add(sub(p, sub(s, sb)), sub(mone, sb));
+    const float2 t = lane2::add(lane2::add(se, pe), mul(mul(bc(2.f), uh), ul));
+    const float2 u2m = lane2::add(s, t);
+    const float2 tb = sub(u2m, s);
+    const float2 u2m_lo = lane2::add(sub(s, sub(u2m, tb)), sub(t, tb));
+    const float2 sq = mul(u2m, u2m);
+    const float2 u2 = lane2::add(u2m, one);
+    const float2 w = mul(u2m, uh);
+    const float2 f = sub(kmul(k.k_ieps, w), kmul(k.k_eps, lap));
+    as.add(sq, lane2::add(fma(u2m, u2m, neg(sq)), mul(mul(bc(2.f), u2m), u2m_lo)));
+    af.add(mul(f, f), bc(0.f));
     if (euler) {
-        g = k.k_K2.mul((3.f * u2 - 1.f) * f);
+        g = kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), one), f));
         h = f;
     } else {
-        g = -(k.k_K3.mul(w) + k.k_K2.mul((3.f * u2 - D - 1.f) * f));
+        g = neg(lane2::add(kmul(k.k_K3, w), kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), bc(2.5f)), f))));
         h = w;
     }
 }

@@ -247,6 +247,8 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
                 // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
                 const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + row0 * M;
                 float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + row0 * M : nullptr;
+                Acc2 as2, af2;
+                PSum2 ag2, ah2;
                 for (int it = tid; it < RPC * M; it += NT) {
                     const int q = it % M, j = it / M;
                     const int ui = j * M + q;  // row j, x slot q (the field is stored in x-slot order)
@@ -254,17 +256,20 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
                     C* pu = S + j * LP + q;
                     C* pl = S + (RPC + j) * LP + q;
                     const C dd = *pu, ll = *pl;
-                    const float2 u0 = ff_add_f(make_float2(Uv.x, Uv.y), dd.x);
-                    const float2 u1 = ff_add_f(make_float2(Uv.z, Uv.w), dd.y);
-                    if (Uo) Uo[ui] = make_float4(u0.x, u0.y, u1.x, u1.y);
-                    C g, h;
-                    fused_point_u(k, euler, u0.x, u0.y, ll.x, as, af, g.x, h.x);
-                    fused_point_u(k, euler, u1.x, u1.y, ll.y, as, af, g.y, h.y);
-                    ag.add(g.x); ag.add(g.y);
-                    ah.add(h.x); ah.add(h.y);
+                    float2 uh, ul;
+                    ff_add_f2(Uv, dd, uh, ul);
+                    if (Uo) Uo[ui] = make_float4(uh.x, ul.x, uh.y, ul.y);
+                    float2 g, h;
+                    fused_point_u2(k, euler, uh, ul, ll, as2, af2, g, h);
+                    ag2.add(g);
+                    ah2.add(h);
                     *pu = g;
                     *pl = h;
                 }
+                as.v = as2.part();
+                af.v = af2.part();
+                ag.s = ag2.s.x + ag2.s.y;
+                ah.s = ah2.s.x + ah2.s.y;
             } else {
                 for (int it = tid; it < RPC * M; it += NT) {
                     const int q = it % M, j = it / M;

@@ -156,6 +156,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
         const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
         float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
                                       : nullptr;
+        Acc2 as2, af2;
+        PSum2 ag2, ah2;
         for (int it = tid; it < NH * M; it += NT) {
             const int qq = it % M, r = it / M;
             const int ui = tidx<NY>(rank * NH + r) * M + qq;  // row y, x slot qq (stored in x-slot order)
@@ -163,17 +165,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             C* pu = S + r * PX + qq;
             C* pl = pu + M;
             const C dd = *pu, ll = *pl;
-            const float2 u0 = ff_add_f(make_float2(Uv.x, Uv.y), dd.x);
-            const float2 u1 = ff_add_f(make_float2(Uv.z, Uv.w), dd.y);
-            if (Uo) Uo[ui] = make_float4(u0.x, u0.y, u1.x, u1.y);
-            C g, h;
-            fused_point_u(k, euler, u0.x, u0.y, ll.x, as, af, g.x, h.x);
-            fused_point_u(k, euler, u1.x, u1.y, ll.y, as, af, g.y, h.y);
-            ag.add(g.x); ag.add(g.y);
-            ah.add(h.x); ah.add(h.y);
+            float2 uh, ul;
+            ff_add_f2(Uv, dd, uh, ul);
+            if (Uo) Uo[ui] = make_float4(uh.x, ul.x, uh.y, ul.y);
+            float2 g, h;
+            fused_point_u2(k, euler, uh, ul, ll, as2, af2, g, h);
+            ag2.add(g);
+            ah2.add(h);
             *pu = g;
             *pl = h;
         }
+        as.v = as2.part();
+        af.v = af2.part();
+        ag.s = ag2.s.x + ag2.s.y;
+        ah.s = ah2.s.x + ah2.s.y;
         auto pv = as.part();
         decltype(pv) vv[4] = {pv, af.part(), ag.part(), ah.part()};
         xy_sums_finalize<T, 4>(I, ctrl, p, 2 * z + rank, 2 * p.nz, vv, red, a.role, true);
