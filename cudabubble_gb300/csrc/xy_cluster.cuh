@@ -158,10 +158,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
                                       : nullptr;
         Acc2 as2, af2;
         PSum2 ag2, ah2;
+        // row y, x slot qq of slot `it` (the field is stored in x-slot order); each
+        // iteration's U load is issued one iteration ahead
+        auto uidx = [&](int it) { return tidx<NY>(rank * NH + it / M) * M + it % M; };
+        float4 Unext = tid < NH * M ? __ldg(Us + uidx(tid)) : make_float4(0.f, 0.f, 0.f, 0.f);
         for (int it = tid; it < NH * M; it += NT) {
             const int qq = it % M, r = it / M;
-            const int ui = tidx<NY>(rank * NH + r) * M + qq;  // row y, x slot qq (stored in x-slot order)
-            const float4 Uv = __ldg(Us + ui);
+            const int ui = uidx(it);
+            const float4 Uv = Unext;
+            if (it + NT < NH * M) Unext = __ldg(Us + uidx(it + NT));
             C* pu = S + r * PX + qq;
             C* pl = pu + M;
             const C dd = *pu, ll = *pl;
