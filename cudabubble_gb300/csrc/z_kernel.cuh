@@ -114,6 +114,12 @@ template <> struct State<float> {
     }
 };
 
+// resident CTAs per SM the z pass is compiled for (its register cap); the pass waits
+// on global loads, so more resident warps hide more of them
+#ifndef CB_Z_MINB
+#define CB_Z_MINB 4
+#endif
+
 // Mode groups: each z_kernel instance compiles only its group's stage code, so
 // the ETD-RK2 instance does not carry the registers of the ETD-RK4 combine.
 enum ZGroup { ZG_ETD2 = 0, ZG_ETD4 = 1, ZG_EULER = 2, ZG_PLAIN = 3 };
@@ -124,7 +130,7 @@ __host__ __device__ constexpr int zgroup_of(int mode) {
 }
 
 template <class T, int NZ, int TX, int NT, int MG>
-__global__ void __launch_bounds__(NT, 4) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+__global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
