@@ -80,3 +80,50 @@ def test_create_fails_loudly_without_gpu(cblib):
     with pytest.raises(capi.CBError) as ei:
         capi.Stepper(p)
     assert ei.value.code == capi.CB_ECUDA
+
+
+C_PROGRAM = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "cbstep.h"
+int main(int argc, char** argv) {
+    cb_params p;
+    cb_params_default(&p);
+    if (cb_params_from_ini_line(argv[1], &p) != CB_OK) { printf("ERR %s\n", cb_last_error()); return 1; }
+    printf("%d %d %d %.17g %d %d\n", p.nx, p.ny, p.nz, cb_params_eps(&p), p.method, p.precision);
+    printf("%zu %zu %zu %zu %zu\n", sizeof(cb_params), offsetof(cb_params, reject_tol), offsetof(cb_params, spont_c),
+           sizeof(cb_run_stats), sizeof(cb_adjust_stats));
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler", ["gcc", "g++"])
+def test_header_compiles_and_links_from_c_and_cpp(cblib, tmp_path, compiler):
+    """The drop-in boundary from the reference's own side: a C (and C++) caller
+    includes include/cbstep.h, links libcbstep.so and parses the ini line; the
+    struct layouts agree with the ctypes mirror the tests use."""
+    import ctypes
+    import shutil
+    import subprocess
+    from cudabubble_gb300 import capi
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not installed")
+    src = tmp_path / ("t.c" if compiler == "gcc" else "t.cpp")
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "t"
+    libdir = os.path.dirname(capi.LIB_PATH)
+    r = subprocess.run([compiler, "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe), "-L", libdir, "-lcbstep", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    line = open(os.path.join(ROOT, "tests", "golden", "ini0_line.txt")).read().strip()
+    out = subprocess.run([str(exe), line], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    l1, l2 = out.stdout.split("\n")[:2]
+    p = capi.params_from_ini(line)
+    f = l1.split()
+    assert (int(f[0]), int(f[1]), int(f[2])) == (p.nx, p.ny, p.nz)
+    assert float(f[3]) == capi.lib().cb_params_eps(ctypes.byref(p))
+    sizes = [int(v) for v in l2.split()]
+    assert sizes == [ctypes.sizeof(capi.cb_params), capi.cb_params.reject_tol.offset, capi.cb_params.spont_c.offset,
+                     ctypes.sizeof(capi.cb_run_stats), ctypes.sizeof(capi.cb_adjust_stats)]
