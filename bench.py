@@ -234,6 +234,22 @@ def served(duration_s: float, max_steps: int):
                     "continuous batching, FP32 form; latency = finish - arrival"}
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest x over the ranks (the slowest replica's time); x itself on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(points: int, steps: int, seconds: float, world: int) -> float:
+    """Whole-job grid-point*steps/s: each of the `world` ranks advances its own replica
+    of the workload (no exchange between replicas), timed by the slowest."""
+    return world * points * steps / seconds
+
+
 def run_ours(args, rank: int, world: int):
     import torch
     from cudabubble_gb300 import capi
@@ -265,14 +281,11 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.synchronize()
     sc = st.scalars()
     ms = r["device_ms"]
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     steps = sc["steps"]
     attempts = r["attempts"]
     rejects = sc["rejects"]
-    value = world * N * steps / (ms / 1e3)
+    value = job_throughput(N, steps, ms / 1e3, world)
     ref_E = golden_energy(steps)
     rel_E = abs(sc["E"] - ref_E) / abs(ref_E) if ref_E else None
 
@@ -308,14 +321,16 @@ def run_ours(args, rank: int, world: int):
 
     # end to end through the C ABI with host buffers: set_phi(host) + run(K) + get_phi(host)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     st.set_phi(p0)
     rr = st.run(args.steps)
     out = st.get_phi()
     sc2 = st.scalars()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_steps = sc2["steps"]
-    e2e = {"value": world * N * e2e_steps / e2e_s, "unit": UNIT,
+    e2e = {"value": job_throughput(N, e2e_steps, e2e_s, world), "unit": UNIT,
            "h2d_bytes_per_step": int(p0.nbytes / max(e2e_steps, 1)),
            "d2h_bytes_per_step": int((out.nbytes + 120) / max(e2e_steps, 1)),
            "what": "cb_set_phi(host phi0) + cb_run(K) + cb_get_phi(host) + cb_scalars_get, wall clock"}

@@ -316,6 +316,18 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
         C un;
         float2 dv = make_float2(0.f, 0.f);  // FP32 form: us - state, the transformed part of u
         if constexpr (sizeof(T) == 4) {
+            // the table row (8 floats, 32-byte aligned) in one or two vector loads
+            float cfr[8];
+            {
+                const float4 q0 = __ldg(reinterpret_cast<const float4*>(cf));
+                cfr[0] = q0.x; cfr[1] = q0.y; cfr[2] = q0.z; cfr[3] = q0.w;
+                if constexpr (g4) {
+                    const float4 q1 = __ldg(reinterpret_cast<const float4*>(cf) + 1);
+                    cfr[4] = q1.x; cfr[5] = q1.y; cfr[6] = q1.z; cfr[7] = q1.w;
+                } else {
+                    cfr[4] = cfr[5] = cfr[6] = cfr[7] = 0.f;
+                }
+            }
             // FP32 form: N-hat = N'-hat + c_lin u-hat (misc_kernels.cuh, lin_coef).  nh is
             // N'-hat; the c_lin terms act on the exact double-float spectra through the
             // table, written with the stage increments d_a = a - phi, d_b = b - phi.
@@ -325,23 +337,23 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
                     if constexpr (!(g2 || g4)) break;
                     const State<T> sp = State<T>::load(phat, g);
                     if (reuse) {
-                        nh = Nu[g];
+                        nh = __ldg(Nu + g);
                     } else {
                         add_lam(nh, sp.work());
                         Nu[g] = nh;
                     }
-                    us = sp.axpy(cf[0], cmk<C>(cf[1] * nh.x, cf[1] * nh.y));
+                    us = sp.axpy(cfr[0], cmk<C>(cfr[1] * nh.x, cfr[1] * nh.y));
                     us.store(ah, g);
                     dv = us.diff(sp);
                     break;
                 }
                 case Z_ETD2_S2: {  // phi' = a (+) (c2 (N'_a - N'_u) + c2 c_lin d_a)
                     if constexpr (!g2) break;
-                    const C nu = Nu[g];
+                    const C nu = __ldg(Nu + g);
                     const State<T> sa = State<T>::load(ah, g), sp = State<T>::load(phat, g);
                     add_lam(nh, sa.work());
                     const float2 da = sa.diff(sp);
-                    us = sa.add(cmk<C>(fmaf(cf[3], da.x, cf[2] * (nh.x - nu.x)), fmaf(cf[3], da.y, cf[2] * (nh.y - nu.y))));
+                    us = sa.add(cmk<C>(fmaf(cfr[3], da.x, cfr[2] * (nh.x - nu.x)), fmaf(cfr[3], da.y, cfr[2] * (nh.y - nu.y))));
                     us.store(cand, g);
                     dv = us.diff(sp);
                     break;
@@ -352,7 +364,7 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
                     if constexpr (!g4) break;
                     const State<T> sp = State<T>::load(phat, g), sa = State<T>::load(ah, g);
                     const float2 da = sa.diff(sp);
-                    const T emh = cf[0], ch = cf[1], chcl = cf[6];
+                    const T emh = cfr[0], ch = cfr[1], chcl = cfr[6];
                     // increment of b = phi (+) (em'_h phi + c_h N'_a + c_h c_lin d_a)
                     auto inc_b = [&](C na) {
                         return cmk<C>(fmaf(chcl, da.x, ch * na.x), fmaf(chcl, da.y, ch * na.y));
@@ -364,7 +376,7 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
                         dv = us.diff(sp);
                         break;
                     }
-                    const C na = Na[g], nu = Nu[g];
+                    const C na = __ldg(Na + g), nu = __ldg(Nu + g);
                     const C ib = inc_b(na);
                     const float2 db = make_float2(fmaf(emh, sp.hi.x, ib.x), fmaf(emh, sp.hi.y, ib.y));
                     const C spw = sp.work();
@@ -382,17 +394,17 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
                     }
                     // phi' = phi (+) (em'_4 phi + f1 N'_1 + f2 (N'_a + N'_b) + f3 N'_c
                     //                 + c_lin (f1 d_1 + f2 (d_a + d_b) + f3 d_c))
-                    const C nb = Nb[g];
+                    const C nb = __ldg(Nb + g);
                     const C ic = inc_c(nb);
                     const float2 dc = make_float2(da.x + fmaf(emh, sa.hi.x, ic.x), da.y + fmaf(emh, sa.hi.y, ic.y));
                     add_lam(nh, cmk<C>(spw.x + dc.x, spw.y + dc.y));  // c = phi + d_c
-                    const T f1 = cf[3], f2 = cf[4], f3 = cf[5], cl = cf[7];
+                    const T f1 = cfr[3], f2 = cfr[4], f3 = cfr[5], cl = cfr[7];
                     const C n1 = ref4 ? na : nu;
                     const float2 d1 = ref4 ? da : make_float2(0.f, 0.f);
                     const C inc = cmk<C>(
                         fmaf(cl, f1 * d1.x + f2 * (da.x + db.x) + f3 * dc.x, f1 * n1.x + f2 * (na.x + nb.x) + f3 * nh.x),
                         fmaf(cl, f1 * d1.y + f2 * (da.y + db.y) + f3 * dc.y, f1 * n1.y + f2 * (na.y + nb.y) + f3 * nh.y));
-                    us = sp.axpy(cf[2], inc);
+                    us = sp.axpy(cfr[2], inc);
                     us.store(cand, g);
                     dv = us.diff(sp);
                     break;
