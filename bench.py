@@ -198,10 +198,21 @@ def plain_fp64(steps: int):
             "what": "CB_FP64 (FP64 transforms, split y/x plane passes at 128^2), same workload, steps 1..K"}
 
 
-def batched(steps: int):
-    """Workload config 4 through cb_batch (FP32 form)."""
+# cb_params.xy_split codes
+PATH_NAMES = ["auto", "split", "single", "cluster"]
+
+
+def batched(steps: int, tune: bool = False):
+    """Workload config 4 through cb_batch (FP32 form); with `tune`, the xy path of each
+    size class is chosen by cb_autotune first, else by the size rule."""
     from cudabubble_gb300 import capi, workloads
     plist, phis = workloads.batched()
+    tuned = {}
+    if tune:
+        first = {}
+        for p, ph in zip(plist, phis):
+            first.setdefault((p.nx, p.nz, p.method, p.precision), ph)
+        tuned = capi.tune_xy_paths(plist, lambda p: first[(p.nx, p.nz, p.method, p.precision)])
     b = capi.Batch(plist)
     for i, ph in enumerate(phis):
         b.set_phi(i, ph)
@@ -213,15 +224,23 @@ def batched(steps: int):
     b.close()
     return {"value": pts / (r["device_ms"] / 1e3), "unit": UNIT, "instances": len(plist),
             "grid_points": int(sum(p.nx * p.ny * p.nz for p in plist)), "steps_per_instance": steps,
+            "xy_paths": {f"{k[0]}x{k[0]}x{k[1]}": PATH_NAMES[v] for k, v in tuned.items()} or "size rule",
             "attempts": r["attempts"], "device_ms": r["device_ms"],
             "what": "config 4: 64 vesicles, grids U{32,48,64,96,128}^3 (seed 4), alpha x U[0.6,0.95], ETD-RK2 "
-                    "per-instance adaptive dt, one CUDA graph per attempt over all size classes, FP32 form"}
+                    "per-instance adaptive dt, one CUDA graph per attempt over all size classes, FP32 form; "
+                    + ("xy path per size class chosen by cb_autotune" if tune else "xy path by the size rule")}
 
 
-def served(duration_s: float, max_steps: int):
-    """Workload config 5 through cb_serve_trace (FP32 form, 150 GB budget)."""
-    from cudabubble_gb300 import capi, workloads
+def served(duration_s: float, max_steps: int, tune: bool = False):
+    """Workload config 5 through cb_serve_trace (FP32 form, 150 GB budget); `tune` as in
+    batched()."""
+    from cudabubble_gb300 import capi, shapes, workloads
     reqs = workloads.served(duration_s=duration_s, max_steps=max_steps)
+    tuned = {}
+    if tune:
+        tuned = capi.tune_xy_paths([r.params for r in reqs],
+                                   lambda p: shapes.ellipsoid(p.nx, p.nz, shapes.eps_rule(p.epssize, p.nx),
+                                                              (1.6, 1.6, 0.8)))
     res, stats, _ = capi.serve_trace(reqs, 150 * 10 ** 9, max_slots_per_class=64, quantum=4)
     lat = np.array([r["latency_s"] for r in res])
     conv = sum(1 for r in res if r["status"] == 5)
@@ -229,6 +248,7 @@ def served(duration_s: float, max_steps: int):
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "value": stats["point_steps"] / stats["wall_s"], "unit": UNIT, "wall_s": stats["wall_s"],
             "peak_bytes": stats["peak_bytes"],
+            "xy_paths": {f"{k[0]}x{k[0]}x{k[1]}": PATH_NAMES[v] for k, v in tuned.items()} or "size rule",
             "what": f"config 5: Poisson 200 req/s for {duration_s:g} s (seed 5), grids {{32..256}}^3 weighted "
                     f"30/25/20/15/7/3 %, ETD-RK2 to |dE/E|<1e-8 capped at {max_steps} steps, 150 GB budget, "
                     "continuous batching, FP32 form; latency = finish - arrival"}
@@ -250,6 +270,15 @@ def job_throughput(points: int, steps: int, seconds: float, world: int) -> float
     return world * points * steps / seconds
 
 
+def xy_path_config(tune) -> dict:
+    """The xy path of the headline handle: the autotuner's choice and timings, or the size
+    rule (the two-CTA cluster pass at 128^2 planes)."""
+    if tune is None:
+        return {"xy_path": "size rule (cluster)"}
+    return {"xy_path": PATH_NAMES[tune["path"]],
+            "xy_path_ms_per_attempt": {PATH_NAMES[k]: round(v, 4) for k, v in tune["timed"].items()}}
+
+
 def run_ours(args, rank: int, world: int):
     import torch
     from cudabubble_gb300 import capi
@@ -267,9 +296,11 @@ def run_ours(args, rank: int, world: int):
     params = capi.default_params(nx=N_GRID, ny=N_GRID, nz=N_GRID, epssize=EPSSIZE, method=capi.CB_ETD2,
                                  precision=capi.CB_FP32, time_step=DT0, fixed_time_step=0.0, M1=1e4, M2=1e4)
     st = capi.Stepper(params)
-    # warm-up on the same workload, then reload phi0
+    # warm-up on the same workload (and, with --tune, the xy path picked by the autotuner),
+    # then phi0 again
     st.set_phi(p0)
     st.run(args.warmup)
+    tune = st.autotune(10) if args.tune else None
     st.set_phi(p0)
     if world > 1:
         torch.distributed.barrier()
@@ -341,7 +372,8 @@ def run_ours(args, rank: int, world: int):
            "dtype": "f32 (FFT + pointwise), f64 reductions / scalars / energy test", "data": "synthetic",
            "config": {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2", "attempts": attempts,
                       "rejects": rejects, "l2": "flushed between attempts (256 MiB memset, outside timed events)",
-                      "parallelism": "replicas" if world > 1 else "single GPU", "points": N},
+                      "parallelism": "replicas" if world > 1 else "single GPU", "points": N,
+                      **xy_path_config(tune)},
            "accuracy": {"E_step_K": sc["E"], "E_reference_fp64_cufft": ref_E, "rel_E_error": rel_E},
            "e2e": e2e, "gpu_launches": attempts * LAUNCHES_PER_ATTEMPT, "roofline": roofline,
            "wall_s_timed_region": wall}
@@ -358,6 +390,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--tune", action="store_true", help="choose xy paths with cb_autotune (default: size rule)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -389,8 +422,8 @@ def main():
         pf = plain_fp64(args.steps)
         res["plain_fp64"] = pf
         res["speedup_fp32_over_plain_fp64"] = res["value"] / pf["value"]
-        res["batched"] = batched(min(args.steps, 60))
-        res["served"] = served(2.0, 200)
+        res["batched"] = batched(min(args.steps, 60), args.tune)
+        res["served"] = served(2.0, 200, args.tune)
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline()

@@ -20,6 +20,7 @@ CB_EULER, CB_ETD2, CB_ETD4 = 0, 1, 2
 CB_FP64, CB_FP32 = 0, 1
 (CB_FIELD_PHI, CB_FIELD_FD, CB_FIELD_LAP, CB_FIELD_F, CB_FIELD_G0, CB_FIELD_NLD, CB_FIELD_DX, CB_FIELD_DY,
  CB_FIELD_DZ, CB_FIELD_S, CB_FIELD_NLD_HAT, CB_FIELD_RHS) = range(12)
+XYP_AUTO, XYP_SPLIT, XYP_SINGLE, XYP_CLUSTER = range(4)
 (CB_RUNNING, CB_DONE_TARGET, CB_DONE_DT_UNDERFLOW, CB_DONE_SMALL_ENERGY, CB_DONE_NONFINITE, CB_DONE_CONVERGED,
  CB_DONE_TMAX) = range(7)
 STATUS_NAMES = {0: "running", 1: "target", 2: "dt_underflow", 3: "small_energy", 4: "nonfinite", 5: "converged",
@@ -55,6 +56,10 @@ class cb_run_stats(C.Structure):
 class cb_adjust_stats(C.Structure):
     _fields_ = [("steps", C.c_int), ("attempts", C.c_int), ("status", C.c_int), ("graph_launches", C.c_int),
                 ("t", C.c_double), ("E_start", C.c_double), ("E_end", C.c_double), ("device_ms", C.c_double)]
+
+
+class cb_tune_result(C.Structure):
+    _fields_ = [("path", C.c_int), ("npaths", C.c_int), ("paths", C.c_int * 3), ("ms_per_attempt", C.c_double * 3)]
 
 
 class cb_request(C.Structure):
@@ -97,6 +102,7 @@ SIGNATURES = {
     "cb_set_dt": (C.c_int, [C.c_void_p, C.c_double]),
     "cb_set_loop_state": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
     "cb_shape_adjust": (C.c_int, [C.c_void_p, C.c_int, _P(cb_adjust_stats)]),
+    "cb_autotune": (C.c_int, [C.c_void_p, C.c_int, _P(cb_tune_result)]),
     "cb_synchronize": (C.c_int, [C.c_void_p]),
     "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
@@ -166,6 +172,27 @@ def params_from_ini(line: str) -> cb_params:
     return p
 
 
+def tune_xy_paths(params_list, phi_for, attempts: int = 6) -> dict:
+    """Autotune the xy path once per (grid, method, precision) class of `params_list`
+    and write the choice into each member's ``xy_split`` (members set to 0 only).
+    ``phi_for(p)`` gives a representative initial field for a class; each class is
+    timed on a temporary stepper (``cb_autotune``).  Returns {class key: path}."""
+    chosen = {}
+    for p in params_list:
+        key = (p.nx, p.nz, p.method, p.precision)
+        if p.xy_split != XYP_AUTO:
+            continue
+        if key not in chosen:
+            st = Stepper(p)
+            try:
+                st.set_phi(phi_for(p))
+                chosen[key] = st.autotune(attempts)["path"]
+            finally:
+                st.close()
+        p.xy_split = chosen[key]
+    return chosen
+
+
 def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
@@ -230,6 +257,12 @@ class Stepper:
     def set_loop_state(self, t: float, dt: float, alpha: float, beta: float):
         """Resume a run: accepted time, dt and volume / area targets (after set_phi)."""
         check(lib().cb_set_loop_state(self.h, t, dt, alpha, beta))
+
+    def autotune(self, attempts: int = 20) -> dict:
+        """Time each xy path this handle can run and keep the fastest."""
+        r = cb_tune_result()
+        check(lib().cb_autotune(self.h, attempts, C.byref(r)))
+        return {"path": r.path, "timed": {r.paths[i]: r.ms_per_attempt[i] for i in range(r.npaths)}}
 
     def shape_adjust(self, max_steps: int = 0) -> dict:
         """belastic::shape_adjust (belastic.cpp:174-284) on the current state."""

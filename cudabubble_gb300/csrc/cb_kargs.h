@@ -7,6 +7,10 @@ namespace cb {
 // nonlinear partials G'', w of the same state in one pass; the penalty terms
 // enter in the next z pass, once the sums have given lambda.
 enum XYMode { XY_REDUCE_FULL = 0, XY_REDUCE_S = 1, XY_NONLIN = 2, XY_FUSED = 3, XY_INV_PLAIN = 4, XY_FWD_PLAIN = 5 };
+// how an xy pass runs (cb_params.xy_split): the size rule (one CTA per plane where two
+// fields fit, two-CTA clusters for the FP32 fused pass, else split), the split y/x
+// passes, one CTA per plane, or two-CTA clusters for the FP32 fused pass
+enum XYPath { XYP_AUTO = 0, XYP_SPLIT = 1, XYP_SINGLE = 2, XYP_CLUSTER = 3 };
 
 struct XYArgs {
     int mode;

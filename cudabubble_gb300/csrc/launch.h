@@ -14,11 +14,13 @@ template <class T> struct Launch {
     static bool xy_plain_supported(int nx);  // plain transforms
     static bool xy_single(int nx, int nf);   // one CTA per plane holds nf fields
     static bool xy_split_supported(int nx);
+    static bool xy_cluster_ok(int nx);       // FP32 fused pass on two-CTA clusters
     static int xy_rows_per_cta(int nx);      // split path: rows of the x pass per CTA
     static int z_tile();
-    // split: 1 forces the split plane path, 0 uses it only where a plane does not fit one CTA
+    // path: an XYPath.  XYP_SINGLE falls back to the split passes where one plane does not
+    // fit a CTA; XYP_CLUSTER applies to the FP32 fused pass and is the size rule otherwise
     static cudaError_t xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
-                          int split = 0);
+                          int path = XYP_AUTO);
     static cudaError_t z(int nz, const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s);
     static cudaError_t decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s);
     static cudaError_t coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw = 1);

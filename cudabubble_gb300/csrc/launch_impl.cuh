@@ -67,10 +67,11 @@ static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArg
 }
 
 template <class T, int NX>
-static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
+                         bool allow_cluster) {
     const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED;
     if constexpr (xyc_ok<T, NX>()) {
-        if (a.mode == XY_FUSED) return xyc_go<T, NX>(d, ninst, nzmax, a, s);
+        if (a.mode == XY_FUSED && allow_cluster) return xyc_go<T, NX>(d, ninst, nzmax, a, s);
     }
     if constexpr (XYCfg<T, NX>::ok) {
         if (a.mode == XY_NONLIN || a.mode == XY_FUSED) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN>(d, ninst, nzmax, a, s);
@@ -188,6 +189,18 @@ static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a
 
 #define CB_XY_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128)
 #define CB_Z_SIZES(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+// sizes the two-CTA cluster pass is built for (where its plane fits: 72.7 KB per CTA at
+// 128^2, ~157 KB at 192^2)
+#define CB_XYC_SIZES(X) X(64) X(96) X(128) X(192)
+
+template <class T> bool Launch<T>::xy_cluster_ok(int nx) {
+    switch (nx) {
+#define CASE(n) case n: return xyc_ok<T, n>();
+        CB_XYC_SIZES(CASE)
+#undef CASE
+        default: return false;
+    }
+}
 
 template <class T> bool Launch<T>::xy_single(int nx, int nf) {
     switch (nx) {
@@ -220,11 +233,19 @@ template <class T> int Launch<T>::z_tile() { return ztile<T>(); }
 
 template <class T>
 cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
-                          int split) {
+                          int path) {
     const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED) ? 2 : 1;
-    if (!split && xy_single(nx, nf)) {
+    if (path == XYP_CLUSTER && a.mode == XY_FUSED && xy_cluster_ok(nx)) {
         switch (nx) {
-#define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s);
+#define CASE(n) case n: if constexpr (xyc_ok<T, n>()) return xyc_go<T, n>(d, ninst, nzmax, a, s); break;
+            CB_XYC_SIZES(CASE)
+#undef CASE
+            default: break;
+        }
+    }
+    if (path != XYP_SPLIT && xy_single(nx, nf)) {
+        switch (nx) {
+#define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s, path != XYP_SINGLE);
             CB_XY_SIZES(CASE)
 #undef CASE
             default: return cudaErrorInvalidValue;
@@ -292,6 +313,7 @@ cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_
     template bool cb::Launch<T>::xy_plain_supported(int);                                                           \
     template bool cb::Launch<T>::xy_single(int, int);                                                               \
     template bool cb::Launch<T>::xy_split_supported(int);                                                           \
+    template bool cb::Launch<T>::xy_cluster_ok(int);                                                                \
     template int cb::Launch<T>::xy_rows_per_cta(int);                                                               \
     template cudaError_t cb::Launch<T>::xy(int, const cb::InstT<T>*, int, int, const cb::XYArgs&, cudaStream_t, int); \
     template cudaError_t cb::Launch<T>::decide(const cb::InstT<T>*, int, int, cudaStream_t);                        \

@@ -194,7 +194,8 @@ __global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurat
 //             grow dt every grow_every accepted steps (belastic.cpp:644-651, :376-378)
 //   corr:     fixed dt with M != 0 -- correct alpha/beta and redo the step once
 //             from the kept state (belastic.cpp:670-691)
-//   raw:      accept unconditionally (a single reference step body)
+//   raw:      1: accept unconditionally (a single reference step body);
+//             2: accept nothing and keep dt (attempts timed by the autotuner)
 // Exit tests follow belastic.cpp:400-428 (Euler) and :712-740 (ETD).
 template <class T>
 __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
@@ -205,6 +206,10 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     const Params& p = I.p;
     if (c->done) return;
     c->attempts++;
+    if (raw == 2) {  // a timing attempt: the state, dt and counters stay, the next attempt is fresh
+        c->fresh = 1;
+        return;
+    }
     const Scal cs = c->sc[R_CAND];
     const double E1 = cs.E;
     c->E_last_attempt = E1;

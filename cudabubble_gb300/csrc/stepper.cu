@@ -148,6 +148,10 @@ int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double be
     CB_H(h);
     return h->impl->set_loop_state(t, dt, alpha, beta);
 }
+int cb_autotune(cb_handle* h, int attempts, cb_tune_result* out) {
+    CB_H(h);
+    return h->impl->autotune(attempts, out);
+}
 int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st) {
     CB_H(h);
     return h->impl->shape_adjust(max_steps, st);

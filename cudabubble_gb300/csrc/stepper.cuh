@@ -153,7 +153,8 @@ inline int make_params(const cb_params& u, Eff& e) {
     p.kmax = (p.nx / 2) * (p.nx / 2) + (p.ny / 2) * (p.ny / 2) + (p.nz / 2) * (p.nz / 2);
     const bool euler = u.method == CB_EULER;
     p.grow_every = u.grow_every > 0 ? u.grow_every : 4;
-    p.split = u.xy_split ? 1 : 0;
+    if (u.xy_split < XYP_AUTO || u.xy_split > XYP_CLUSTER) return fail(CB_EINVAL, "xy_split %d: 0..3", u.xy_split);
+    p.split = u.xy_split;
     p.grow_factor = u.grow_factor > 0 ? u.grow_factor : (euler ? 1.4 : 2.0);
     p.dt_cap = u.dt_cap > 0 ? u.dt_cap : (euler ? 1e300 : 1e-3);
     p.cap_probe = u.cap_probe > 0 ? u.cap_probe : (euler ? 0.0 : 1.4);
@@ -207,6 +208,7 @@ struct Handle {
     virtual int set_dt(double dt) = 0;
     virtual int set_loop_state(double t, double dt, double alpha, double beta) = 0;
     virtual int shape_adjust(int max_steps, cb_adjust_stats* st) = 0;
+    virtual int autotune(int attempts, cb_tune_result* out) = 0;
     virtual int sync() = 0;
     virtual long long bytes() const = 0;
     virtual int run_timed(int nsteps, long long flush_bytes, double* ms, int* attempts) = 0;
@@ -222,7 +224,7 @@ enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, 
 // event pair brackets every launch and is appended as (kind, start, end).
 template <class T>
 inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, int ninst, int ntiles, int accurate,
-                                 bool raw, int split, cudaStream_t s,
+                                 int raw, int split, cudaStream_t s,
                                  std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
     cudaError_t r = cudaSuccess;
     auto timed = [&](int kind, auto&& fn) {
@@ -317,7 +319,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             break;
     }
     }
-    timed(K_DECIDE, [&]() { return Launch<T>::decide(d, ninst, raw ? 1 : 0, s); });
+    timed(K_DECIDE, [&]() { return Launch<T>::decide(d, ninst, raw, s); });
     return r;
 }
 
@@ -326,7 +328,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
 // every other field is one complex T per mode.
 // the split plane path is used for some xy mode of this precision and grid
 template <class T> inline bool uses_split(const Params& p) {
-    return p.split || !Launch<T>::xy_single(p.nx, 2) || !Launch<T>::xy_single(p.nx, 1);
+    return p.split == XYP_SPLIT || !Launch<T>::xy_single(p.nx, 2) || !Launch<T>::xy_single(p.nx, 1);
 }
 // per-plane or per-row-block partial sums of the xy reductions
 template <class T> inline size_t xy_part_slots(const Params& p) {
@@ -605,6 +607,79 @@ template <class T> class Stepper final : public Handle {
 
     int sync() override {
         CB_CK(cudaStreamSynchronize(st));
+        return CB_OK;
+    }
+
+    // the xy paths this handle can run: the split passes need the y buffers the arena
+    // holds only where the handle was created for them
+    bool path_ok(int path) const {
+        switch (path) {
+            case XYP_SPLIT: return h.Y[0] != nullptr && Launch<T>::xy_split_supported(p.nx);
+            case XYP_SINGLE: return Launch<T>::xy_single(p.nx, 2);
+            case XYP_CLUSTER: return sizeof(T) == 4 && Launch<T>::xy_cluster_ok(p.nx);
+            default: return false;
+        }
+    }
+
+    // Times one attempt of the handle's method on every xy path it can run and keeps
+    // the fastest.  The timed attempts start from the current state and accept nothing
+    // (decide's timing mode), so state, dt, counters and coefficient tables are as
+    // before; the loop graphs are re-captured for the chosen path.
+    int autotune(int attempts, cb_tune_result* out) override {
+        if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
+        if (attempts < 1) return fail(CB_EINVAL, "attempts must be positive");
+        CB_CK(pull());
+        const Ctrl saved = hc;
+        hc.target = INT_MAX;
+        hc.done = 0;
+        hc.fresh = 1;
+        CB_CK(push());
+        const int keep = p.split;
+        const int cands[3] = {XYP_CLUSTER, XYP_SINGLE, XYP_SPLIT};
+        cb_tune_result r{};
+        r.path = -1;
+        double best = 1e300;
+        cudaEvent_t e0, e1;
+        CB_CK(cudaEventCreate(&e0));
+        CB_CK(cudaEventCreate(&e1));
+        int rc = CB_OK;
+        for (int path : cands) {
+            if (!path_ok(path)) continue;
+            p.split = path;
+            cudaGraphExec_t g = nullptr;
+            rc = capture(2, &g);
+            if (rc) break;
+            for (int i = 0; i < 2; ++i) CB_CK(cudaGraphLaunch(g, st));  // warm-up
+            CB_CK(cudaEventRecord(e0, st));
+            for (int i = 0; i < attempts; ++i) CB_CK(cudaGraphLaunch(g, st));
+            CB_CK(cudaEventRecord(e1, st));
+            CB_CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaGraphExecDestroy(g);
+            const double per = ms / attempts;
+            r.paths[r.npaths] = path;
+            r.ms_per_attempt[r.npaths] = per;
+            r.npaths++;
+            if (per < best) {
+                best = per;
+                r.path = path;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        p.split = r.path >= 0 ? r.path : keep;
+        for (cudaGraphExec_t* gp : {&g_loop, &g_raw, &g_shape})
+            if (*gp) {
+                cudaGraphExecDestroy(*gp);
+                *gp = nullptr;
+            }
+        hc = saved;
+        CB_CK(push());
+        CB_CK(cudaStreamSynchronize(st));
+        if (rc) return rc;
+        if (r.npaths == 0) return fail(CB_EUNSUPPORTED, "no xy path to time");
+        if (out) *out = r;
         return CB_OK;
     }
 
@@ -1082,14 +1157,14 @@ template <class T> class Stepper final : public Handle {
         return CB_OK;
     }
     // prof != nullptr: record an event pair around every launch (profiling; not captured)
-    int enqueue_attempt(bool raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr,
+    int enqueue_attempt(int raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr,
                         int method = -1) {
         cudaError_t r = enqueue_group<T>(method < 0 ? p.method : method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw,
                                          p.split, st, prof);
         if (r != cudaSuccess) return fail(CB_ECUDA, "enqueue attempt: %s", cudaGetErrorString(r));
         return CB_OK;
     }
-    int capture(bool raw, cudaGraphExec_t* out, int method = -1) {
+    int capture(int raw, cudaGraphExec_t* out, int method = -1) {
         cudaGraph_t g = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int rc = enqueue_attempt(raw, nullptr, method);

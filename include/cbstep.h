@@ -92,8 +92,10 @@ typedef struct cb_params {
     int accurate_coefficients; /* -1: default (FP32 form: phi-function series; FP64 form: reference closed forms) */
     double rel_tol;          /* > 0: cb_run stops (CB_DONE_CONVERGED) once an accepted step changes
                                 E by less than rel_tol |E|; not in the reference loops */
-    int xy_split;            /* 1: always use the split (y-column + x-row) plane passes; 0: only where
-                                a plane's two fields do not fit one CTA (FP64 from 128^2, all 192^2+) */
+    int xy_split;            /* xy pass path: 0 the size rule (one CTA per plane where a plane's two fields
+                                fit, two-CTA clusters for the FP32 form from 64^2, else the split passes);
+                                1 the split (y-column + x-row) passes; 2 one CTA per plane; 3 two-CTA
+                                clusters (FP32 form, 64^2..192^2); cb_autotune picks among them */
     int pad0;
     double reject_tol;       /* adaptive loops reject an attempt when E_new > E_old + reject_tol |E_old|;
                                 < 0: default 0, the reference rule (belastic.cpp:653-668), for both forms */
@@ -119,6 +121,13 @@ typedef struct cb_run_stats {
     int graph_launches;
     double device_ms;        /* CUDA-event time of the call's device work */
 } cb_run_stats;
+
+typedef struct cb_tune_result {
+    int path;                /* the chosen xy path (cb_params.xy_split code) */
+    int npaths;              /* paths timed */
+    int paths[3];
+    double ms_per_attempt[3];
+} cb_tune_result;
 
 typedef struct cb_adjust_stats {
     int steps;               /* accepted adjustment steps */
@@ -175,6 +184,11 @@ int cb_set_loop_state(cb_handle* h, double t, double dt, double alpha, double be
  * alpha, beta are taken again from the adjusted state when the parameters' beta <= 0.
  * max_steps > 0 bounds the accepted steps (0: 1,000,000). */
 int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st);
+/* no counterpart in the reference: times `attempts` attempts of the handle's method on
+ * each xy path it can run (2-CTA clusters, one CTA per plane, and the split passes when
+ * the handle was created with them), from the current state without accepting any,
+ * and keeps the fastest for this handle; the state, dt and counters are unchanged */
+int cb_autotune(cb_handle* h, int attempts, cb_tune_result* out);
 int cb_synchronize(cb_handle* h);
 /* HBM bytes held by the handle's stepping state */
 long long cb_handle_bytes(cb_handle* h);
