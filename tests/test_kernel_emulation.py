@@ -1,0 +1,85 @@
+"""Index safety of the stepper's kernels on the CPU.
+
+The kernel headers of cudabubble_gb300/csrc are compiled for the host against a
+CUDA emulation (tests/emu/fake: one OS thread per CUDA thread, real barriers for
+__syncthreads, warp shuffles and cluster barriers) with AddressSanitizer, and one
+FP32-form ETD-RK2 attempt (set-up pass, prologue, coefficient fill, z S1, fused xy
+pass, z S2, fused xy pass, decide) runs on both xy schedules.  Every device buffer
+and every block's shared memory is an exact-size heap allocation, so any access
+outside them fails the test.  The two schedules must also leave the same sums.
+Needs g++ with AddressSanitizer; no GPU."""
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "cudabubble_gb300", "csrc")
+EMU = os.path.join(ROOT, "tests", "emu")
+SMEM_DECL = "extern __shared__ __align__(16) unsigned char smem_raw[];"
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("emu")
+    src = d / "src"
+    src.mkdir()
+    n_decl = 0
+    for f in os.listdir(CSRC):
+        if f.endswith((".cuh", ".h")):
+            t = open(os.path.join(CSRC, f)).read()
+            n_decl += t.count(SMEM_DECL)
+            # the dynamic shared memory of the emulated block
+            t = t.replace(SMEM_DECL, "unsigned char* smem_raw = ::emu::t_blk->smem;")
+            (src / f).write_text(t)
+    assert n_decl >= 4, "every kernel's shared-memory declaration is rewritten"
+    exe = d / "attempt"
+    cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer", "-ffp-contract=off",
+           "-I", os.path.join(EMU, "fake"), "-I", str(src), "-I", os.path.join(ROOT, "include"),
+           os.path.join(EMU, "attempt.cpp"), "-o", str(exe), "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr and "cannot find" in r.stderr:
+        pytest.skip("AddressSanitizer runtime not available")
+    assert r.returncode == 0, r.stderr[-4000:]
+    return str(exe)
+
+
+def run_attempt(exe, n, nz, path):
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1")
+    r = subprocess.run([exe, str(n), str(nz), str(path)], capture_output=True, text=True, env=env, timeout=900)
+    assert "AddressSanitizer" not in r.stderr, r.stderr[-6000:]
+    assert r.returncode == 0, r.stderr[-3000:]
+    vals = {}
+    for line in r.stdout.splitlines():
+        head, *rest = line.split()
+        for k, v in zip(rest[0::2], rest[1::2]):
+            vals[f"{head}.{k}"] = float(v)
+    return vals
+
+
+@pytest.mark.parametrize("n,nz", [(16, 16), (32, 32), (48, 16)])
+def test_single_cta_schedule_in_bounds(harness, n, nz):
+    v = run_attempt(harness, n, nz, 2)
+    assert v["ctrl.attempts"] == 1
+    # every last-CTA counter was reset by the CTA that finalised
+    assert all(v[f"ctrl.{k}"] == 0 for k in ("cnt_xy", "cnt_z"))
+    assert all(abs(v[k]) < float("inf") for k in ("state.V", "state.S", "cand.V", "cand.S"))
+
+
+@pytest.mark.parametrize("n", [64])
+def test_cluster_and_single_schedules_agree(harness, n):
+    """64^2 planes (16 of them): the two-CTA cluster pass (distributed shared
+    memory exchange) and the one-CTA pass in bounds, with the same sums."""
+    a = run_attempt(harness, n, 16, 3)
+    b = run_attempt(harness, n, 16, 2)
+    # V, S, E: the same up to the order of the FP64 partial sums (per plane vs per half plane)
+    for k in ("state.V", "state.S", "state.E", "work.V", "work.S", "cand.V", "cand.S", "cand.E"):
+        assert a[k] == pytest.approx(b[k], rel=1e-9), (k, a, b)
+    # the G'' and w totals, summed per thread in FP32 before the FP64 partials: equal to
+    # the rounding of those per-thread sums
+    for k in ("state.sum_g", "work.sum_g", "work.sum_h"):
+        assert a[k] == pytest.approx(b[k], rel=1e-8, abs=1e-6 * n * n * 16), (k, a, b)
