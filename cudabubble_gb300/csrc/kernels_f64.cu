@@ -46,7 +46,12 @@ static __global__ void real_to_ff_kernel(const double* __restrict__ in, float4* 
     }
 }
 cudaError_t launch_real_to_ff(const double* in, void* out, size_t nrows, int nx, cudaStream_t s) {
-    if (nx < 16 || nx > 256 || nx % 2) return cudaErrorInvalidValue;
+    // only the x lengths tidx_rt knows (a -1 slot would index before the row)
+    switch (nx / 2) {
+        case 8: case 12: case 16: case 24: case 32: case 48: case 64: case 96: case 128: break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (nx % 2) return cudaErrorInvalidValue;
     const size_t n = nrows * (size_t)(nx / 2);
     const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     real_to_ff_kernel<<<blocks, 256, 0, s>>>(in, reinterpret_cast<float4*>(out), nrows, nx);

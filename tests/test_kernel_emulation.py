@@ -8,8 +8,8 @@ pass, z S2, fused xy pass, decide) runs on both xy schedules.  Every device buff
 and every block's shared memory is an exact-size heap allocation, so any access
 outside them fails the test.  The two schedules must also leave the same sums.
 Needs g++ with AddressSanitizer; no GPU."""
+import importlib.util
 import os
-import re
 import shutil
 import subprocess
 
@@ -18,7 +18,6 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "cudabubble_gb300", "csrc")
 EMU = os.path.join(ROOT, "tests", "emu")
-SMEM_DECL = "extern __shared__ __align__(16) unsigned char smem_raw[];"
 
 
 @pytest.fixture(scope="module")
@@ -27,16 +26,11 @@ def harness(tmp_path_factory):
         pytest.skip("g++ not available")
     d = tmp_path_factory.mktemp("emu")
     src = d / "src"
-    src.mkdir()
-    n_decl = 0
-    for f in os.listdir(CSRC):
-        if f.endswith((".cuh", ".h")):
-            t = open(os.path.join(CSRC, f)).read()
-            n_decl += t.count(SMEM_DECL)
-            # the dynamic shared memory of the emulated block
-            t = t.replace(SMEM_DECL, "unsigned char* smem_raw = ::emu::t_blk->smem;")
-            (src / f).write_text(t)
-    assert n_decl >= 4, "every kernel's shared-memory declaration is rewritten"
+    spec = importlib.util.spec_from_file_location("emu_rewrite", os.path.join(EMU, "rewrite.py"))
+    rw = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(rw)
+    # every kernel's shared-memory declaration becomes the emulated block's buffer
+    assert rw.copy_sources(CSRC, str(src)) >= 4
     exe = d / "attempt"
     cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer", "-ffp-contract=off",
            "-I", os.path.join(EMU, "fake"), "-I", str(src), "-I", os.path.join(ROOT, "include"),
