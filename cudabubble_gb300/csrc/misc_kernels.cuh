@@ -8,20 +8,29 @@
 
 namespace cb {
 
-// 1 / m! as compile-time constants (m <= 27)
+// 1 / m! (m <= 27); evaluated by the compiler wherever its argument is a constant
+// expression, which phi_horner below guarantees
 __host__ __device__ constexpr double rfact(int m) { return m <= 1 ? 1.0 : rfact(m - 1) / (double)m; }
+
+// Horner steps j = J .. 0 of the three phi series; the coefficients are constexpr
+// variables, so none is computed at run time (a plain loop left the recursive rfact
+// to the device: hundreds of FP64 divisions per table entry)
+template <int J>
+__device__ __forceinline__ void phi_horner(double z, double& t1, double& t2, double& t3) {
+    constexpr double c1 = rfact(J + 1), c2 = rfact(J + 2), c3 = rfact(J + 3);
+    t1 = fma(t1, z, c1);
+    t2 = fma(t2, z, c2);
+    t3 = fma(t3, z, c3);
+    if constexpr (J > 0) phi_horner<J - 1>(z, t1, t2, t3);
+}
 
 // phi_k(z) = sum_j z^j / (j+k)!, k = 1, 2, 3: Horner series for |z| < 1
 // (24 terms, no divisions), closed forms otherwise
 __device__ inline void phi123(double z, double& p1, double& p2, double& p3) {
     if (fabs(z) < 1.0) {
-        double t1 = rfact(24), t2 = rfact(25), t3 = rfact(26);
-#pragma unroll
-        for (int j = 23; j >= 0; --j) {
-            t1 = fma(t1, z, rfact(j + 1));
-            t2 = fma(t2, z, rfact(j + 2));
-            t3 = fma(t3, z, rfact(j + 3));
-        }
+        constexpr double r24 = rfact(24), r25 = rfact(25), r26 = rfact(26);
+        double t1 = r24, t2 = r25, t3 = r26;
+        phi_horner<23>(z, t1, t2, t3);
         p1 = t1; p2 = t2; p3 = t3;
     } else {
         const double ez = exp(z), iz = 1.0 / z;
