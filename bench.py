@@ -172,9 +172,9 @@ def algorithmic_bytes(n: int, fsize: int, att: int, rej: int):
     }, F
 
 
-# launches of one ETD-RK2 attempt of the FP32 form: prologue, coefficient fill,
+# launches of one ETD-RK2 attempt of the FP32 form: prologue + coefficient fill,
 # z S1, xy FUSED (work), z S2, xy FUSED (candidate), decide
-LAUNCHES_PER_ATTEMPT = 7
+LAUNCHES_PER_ATTEMPT = 6
 
 
 def plain_fp64(steps: int):

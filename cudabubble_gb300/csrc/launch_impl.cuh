@@ -272,10 +272,7 @@ template <class T> cudaError_t Launch<T>::decide(const InstT<T>* d, int ninst, i
     return cudaGetLastError();
 }
 template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw) {
-    prologue_kernel<T><<<(ninst + 127) / 128, 128, 0, s>>>(d, ninst, raw);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    coef_fill_kernel<T><<<dim3(64, ninst), 256, 0, s>>>(d, accurate);
+    prologue_fill_kernel<T><<<dim3(64, ninst), 256, 0, s>>>(d, accurate, raw);
     return cudaGetLastError();
 }
 template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out, size_t n, cudaStream_t s) {

@@ -40,59 +40,73 @@ __device__ inline void phi123(double z, double& p1, double& p2, double& p3) {
     }
 }
 
-// Prologue of every attempt (one thread per instance).  It applies a pending
-// growth of dt (set when the accepted step count reached a multiple of
-// grow_every: belastic.cpp:644-651, :376-378), so the step runs with the grown
-// dt exactly as the reference's loop head grows it, then selects the
-// coefficient table of the attempt's dt from the per-instance cache, marking
-// a slot for filling on a miss.
-template <class T>
-__global__ void prologue_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const InstT<T>& I = insts[i];
-    Ctrl* c = I.ctrl;
-    const Params& p = I.p;
-    if (c->done) return;
+// The prologue's part of the control state: what it reads and what it changes.
+struct ProState {
+    double dt, t, sa_eng;
+    int skip;          // the instance was done on entry: nothing changes
+    int grow_pending, done, status, tab_cur, tab_next;
+    int fill_slot;     // table slot to fill with dt (-1: none)
+};
+
+// Prologue of every attempt, as a function of the control state the previous kernel
+// left (it writes nothing).  It applies a pending growth of dt (set when the accepted
+// step count reached a multiple of grow_every: belastic.cpp:644-651, :376-378), so the
+// step runs with the grown dt exactly as the reference's loop head grows it, then
+// selects the coefficient table of the attempt's dt from the per-instance cache,
+// marking a slot for filling on a miss.
+__device__ inline ProState prologue_state(const Params& p, const Ctrl* c, int raw) {
+    ProState s;
+    s.dt = c->dt;
+    s.t = c->t;
+    s.sa_eng = c->sa_eng;
+    s.grow_pending = c->grow_pending;
+    s.done = c->done;
+    s.status = c->status;
+    s.tab_cur = c->tab_cur;
+    s.tab_next = c->tab_next;
+    s.fill_slot = -1;
+    s.skip = s.done;
+    if (s.skip) return s;
     if (p.sched == SCHED_SHAPE) {
         // loop head of belastic::shape_adjust (belastic.cpp:204-233), run once per
-        // accepted step: advance tcur (c->t) by dt and count the step (the
-        // reference's counter starts at 1 and is raised before the tests); test
-        // convergence when dt > 1e-4 or int(tcur/dt) is a multiple of int(1e-4/dt);
-        // double dt every tenth count.  The quotients are truncated in 64 bits:
-        // the reference's int conversion has no defined result beyond 2^31.
-        if (c->grow_pending) {
-            c->grow_pending = 0;
-            c->t += c->dt;
+        // accepted step: advance tcur (t) by dt and count the step (the reference's
+        // counter starts at 1 and is raised before the tests); test convergence when
+        // dt > 1e-4 or int(tcur/dt) is a multiple of int(1e-4/dt); double dt every
+        // tenth count.  The quotients are truncated in 64 bits: the reference's int
+        // conversion has no defined result beyond 2^31.
+        if (s.grow_pending) {
+            s.grow_pending = 0;
+            s.t += s.dt;
             const int count = c->steps + 2;
-            if (c->dt > 1e-4 || ((long long)(c->t / c->dt)) % ((long long)(1e-4 / c->dt)) == 0) {
-                const double e1 = c->E_state, e0 = c->sa_eng;
+            if (s.dt > 1e-4 || ((long long)(s.t / s.dt)) % ((long long)(1e-4 / s.dt)) == 0) {
+                const double e1 = c->E_state, e0 = s.sa_eng;
                 if (e1 < 100.0 * p.eta || fabs((e0 - e1) / e0) < 0.02) {
-                    c->done = 1;
-                    c->status = ST_CONVERGED;
-                    return;
+                    s.done = 1;
+                    s.status = ST_CONVERGED;
+                    return s;
                 }
-                c->sa_eng = e1;
+                s.sa_eng = e1;
             }
-            if (count % 10 == 0) c->dt *= 2.0;
+            if (count % 10 == 0) s.dt *= 2.0;
         }
-        c->fill_slot = -1;
-        return;
+        return s;
     }
-    if (!raw && c->grow_pending) {
-        const double d0 = c->dt;
-        c->dt = (d0 * p.cap_probe < p.dt_cap) ? d0 * p.grow_factor : p.dt_cap;
-        c->grow_pending = 0;
+    if (!raw && s.grow_pending) {
+        const double d0 = s.dt;
+        s.dt = (d0 * p.cap_probe < p.dt_cap) ? d0 * p.grow_factor : p.dt_cap;
+        s.grow_pending = 0;
     }
-    c->fill_slot = -1;
-    if (p.method == M_EULER) return;
+    if (p.method == M_EULER) return s;
     for (int j = 0; j < kNTab; ++j)
-        if (c->tab_dt[j] == c->dt) { c->tab_cur = j; return; }
-    const int j = c->tab_next;
-    c->tab_next = (j + 1) % kNTab;
-    c->tab_dt[j] = c->dt;
-    c->tab_cur = j;
-    c->fill_slot = j;
+        if (c->tab_dt[j] == s.dt) {
+            s.tab_cur = j;
+            return s;
+        }
+    const int j = s.tab_next;
+    s.tab_next = (j + 1) % kNTab;
+    s.tab_cur = j;
+    s.fill_slot = j;
+    return s;
 }
 
 // Linear part of the ETD nonlinearity, c_lin(k) = eta kappa (D / eps^3 + cx |k|^2 / eps):
@@ -106,7 +120,8 @@ __device__ inline double lin_coef(const Params& p, int k2) {
     return p.eta * kappa * (D * p.d_ieps3 + p.cx * (double)k2 * p.d_ieps);
 }
 
-// Fills the table slot the prologue selected (grid: blocks x instances).
+// Fills this block's share of table `slot` for time step dt (all blocks of the grid
+// together fill entries 0..kmax).
 // L(k) follows Calc.cu:579-606 with c = -cx |k|^2 (kappa = 2, D = 1.5).
 // accurate == 0 evaluates the reference's own closed forms (Calc.cu:446-569);
 // accurate == 1 uses phi-functions, free of the small-|hL| cancellation.
@@ -117,14 +132,7 @@ __device__ inline double lin_coef(const Params& p, int k2) {
 // and its state update is base (+) (em' base + increment) in double-float
 // arithmetic (z_kernel.cuh, State<float>).
 template <class T>
-__global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurate) {
-    const InstT<T>& I = insts[blockIdx.y];
-    Ctrl* ctrl = I.ctrl;
-    const Params& p = I.p;
-    if (p.method == M_EULER || ctrl->done) return;
-    const int slot = ctrl->fill_slot;
-    if (slot < 0) return;
-    const double dt = ctrl->tab_dt[slot];
+__device__ inline void fill_table(const InstT<T>& I, const Params& p, int slot, double dt, int accurate) {
     const double kappa = 2.0, D = 1.5, eps = p.eps, ie = p.d_ieps, ie2 = p.d_ieps2;
     T* tab = I.coef + (size_t)slot * (size_t)(p.kmax + 1) * 8;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx <= p.kmax; idx += gridDim.x * blockDim.x) {
@@ -187,12 +195,40 @@ __global__ void coef_fill_kernel(const InstT<T>* __restrict__ insts, int accurat
             out[1] = (T)ch; out[3] = (T)f1; out[4] = (T)f2; out[5] = (T)f3;
         }
     }
+}
+
+// The prologue and the coefficient table of an attempt in one launch (grid: blocks x
+// instances).  Every block derives the prologue's new state from the state the
+// previous kernel left (prologue_state reads only), fills its share of the table when
+// dt is new, and the last block to finish writes the new state: every block has read
+// the old state before it counts itself done, so none sees a half-written one.
+template <class T>
+__global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int accurate, int raw) {
+    const InstT<T>& I = insts[blockIdx.y];
+    Ctrl* ctrl = I.ctrl;
+    const Params& p = I.p;
+    __shared__ ProState s;
+    __shared__ int last;
+    if (threadIdx.x == 0) s = prologue_state(p, ctrl, raw);
+    __syncthreads();
+    if (s.skip) return;
+    if (s.fill_slot >= 0) fill_table<T>(I, p, s.fill_slot, s.dt, accurate);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned prev = atomicAdd(&ctrl->fill_cnt, 1u);
-        if (prev == gridDim.x - 1) {
+        last = prev == gridDim.x - 1;
+        if (last) {
             ctrl->fill_cnt = 0u;
+            ctrl->dt = s.dt;
+            ctrl->t = s.t;
+            ctrl->sa_eng = s.sa_eng;
+            ctrl->grow_pending = s.grow_pending;
+            ctrl->done = s.done;
+            ctrl->status = s.status;
+            ctrl->tab_cur = s.tab_cur;
+            ctrl->tab_next = s.tab_next;
+            if (s.fill_slot >= 0) ctrl->tab_dt[s.fill_slot] = s.dt;
             ctrl->fill_slot = -1;
         }
     }

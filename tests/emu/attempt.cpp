@@ -6,7 +6,7 @@
 //
 // Sequence (as cb_set_phi and one attempt of the stepper's loop run it):
 //   z Z_INV_STATE (state)   -> xy XY_FUSED (state)
-//   prologue -> coefficient fill -> z S1 -> xy FUSED (work) -> z S2 -> xy FUSED (candidate)
+//   prologue + coefficient fill -> z S1 -> xy FUSED (work) -> z S2 -> xy FUSED (candidate)
 //   -> decide
 // The xy passes run on the schedule given on the command line: 2 = one CTA per plane,
 // 3 = two-CTA clusters.  The sums the passes leave are printed for comparison.
@@ -230,8 +230,7 @@ template <int N, int NZ> int run(int path) {
     z(Z_INV_STATE, R_STATE, GP{});
     xy(XY_FUSED, R_STATE);
     c.E_state = c.sc[R_STATE].E;
-    emu::launch(dim3(1), 128, 0, 1, [&] { prologue_kernel<T>(d, 1, 0); });
-    emu::launch(dim3(64, 1), 256, 0, 1, [&] { coef_fill_kernel<T>(d, 1); });
+    emu::launch(dim3(64, 1), 256, 0, 1, [&] { prologue_fill_kernel<T>(d, 1, 0); });
     z(Z_ETD2_S1, R_WORK, G2{});
     xy(XY_FUSED, R_WORK);
     z(Z_ETD2_S2, R_CAND, G2{});
