@@ -242,14 +242,8 @@ __global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int acc
 //   raw:      1: accept unconditionally (a single reference step body);
 //             2: accept nothing and keep dt (attempts timed by the autotuner)
 // Exit tests follow belastic.cpp:400-428 (Euler) and :712-740 (ETD).
-template <class T>
-__global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const InstT<T>& I = insts[i];
-    Ctrl* c = I.ctrl;
-    const Params& p = I.p;
-    if (c->done) return;
+// The decision on a copy of the control state (decide_kernel writes it back).
+__device__ inline void decide_update(Ctrl* c, const Params& p, int raw) {
     c->attempts++;
     if (raw == 2) {  // a timing attempt: the state, dt and counters stay, the next attempt is fresh
         c->fresh = 1;
@@ -330,6 +324,23 @@ __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw
     // relaxation criterion |dE / E| < rel_tol (no counterpart in the reference loops)
     if (!raw && p.rel_tol > 0.0 && fabs(E1 - E0) < p.rel_tol * fabs(E1)) { c->done = 1; c->status = ST_CONVERGED; }
     if (!raw && p.adaptive && c->steps % p.grow_every == 0) c->grow_pending = 1;
+}
+
+// One thread per instance.  The control state and the parameters are copied in one
+// batch of independent loads, the decision runs on the copies, and the state is
+// written back in one batch: a chain of dependent global loads otherwise sets the
+// kernel's length.
+template <class T>
+__global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const InstT<T>& I = insts[i];
+    Ctrl* g = I.ctrl;
+    Ctrl c = *g;
+    if (c.done) return;
+    const Params p = I.p;
+    decide_update(&c, p, raw);
+    *g = c;
 }
 
 // ---------------------------------------------------------- slow path
