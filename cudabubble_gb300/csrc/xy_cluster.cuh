@@ -50,8 +50,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     const Params& p = I.p;
     const int z = blockIdx.x >> 1;
     const int tid = threadIdx.x;
+    // the control fields and this pass's candidate partial sets in one batch of
+    // independent loads (the state-selected pointers are chosen in registers)
+    const int c_done = ctrl->done, c_part = ctrl->part_state, c_u = ctrl->u_state;
+    const void *p00 = I.P[0][0], *p01 = I.P[0][1], *p10 = I.P[1][0], *p11 = I.P[1][1], *p20 = I.P[2][0],
+               *p21 = I.P[2][1];
     // both CTAs of a cluster hold the same plane of the same instance: they leave together
-    if (z >= p.nz || ctrl->done) return;
+    if (z >= p.nz || c_done) return;
     C* S = reinterpret_cast<C*>(smem_raw);
     C* twM = S + Q::SZ;
     C* twN = twM + M;
@@ -72,9 +77,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     }
     const PC<T> k(p);
     const size_t plane = (size_t)NY * NC;
-    const int set = part_set(ctrl, a.role);
-    const C* P0 = reinterpret_cast<const C*>(I.P[set][0]) + (size_t)z * plane;
-    const C* P2 = reinterpret_cast<const C*>(I.P[set][1]) + (size_t)z * plane;
+    const int set = a.role == R_WORK ? 2 : (a.role == R_STATE ? c_part : 1 - c_part);  // part_set
+    const C* P0 = reinterpret_cast<const C*>(set == 2 ? p20 : (set == 1 ? p10 : p00)) + (size_t)z * plane;
+    const C* P2 = reinterpret_cast<const C*>(set == 2 ? p21 : (set == 1 ? p11 : p01)) + (size_t)z * plane;
     const int c0 = rank * MH;
 
     // ---- load own packed columns (col 0 = kx 0 + i kx M) and the Laplacian partial
@@ -153,8 +158,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
         Acc<T> as, af;
         PSum<T> ag, ah;
         // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
-        const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
-        float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
+        const float4* Us = reinterpret_cast<const float4*>(I.U[c_u]) + (size_t)z * NY * M;
+        float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - c_u]) + (size_t)z * NY * M
                                       : nullptr;
         Acc2 as2, af2;
         PSum2 ag2, ah2;

@@ -142,8 +142,14 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     const int m0 = blockIdx.x * TX;
     const int tid = threadIdx.x;
     if (m0 >= Mc) return;
+    // the control fields and the candidate buffers of this pass in one batch of
+    // independent loads (the state-selected pointer is chosen in registers), so the
+    // CTA does not wait on a chain of dependent loads before its data moves
+    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_ab = ctrl->ab_state;
+    const void* g_a[2] = {I.G[0][0], I.G[1][0]};
+    const void* g_b[2] = {I.G[0][1], I.G[1][1]};
     const bool plain = a.mode == Z_FWD_PLAIN || a.mode == Z_INV_PLAIN;
-    if (!plain && ctrl->done) return;
+    if (!plain && c_done) return;
     const int ntiles = (Mc + TX - 1) / TX;
     constexpr int W = 2 * TX;  // row pitch: field 0 in [0, TX), field 1 in [TX, 2 TX)
     C* S = reinterpret_cast<C*>(smem_raw);
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     for (int i = tid; i < ntw * NZ; i += NT) tw[i] = reinterpret_cast<const C*>(I.twz)[i];
 
     const bool stage1 = a.mode == Z_ETD2_S1 || a.mode == Z_ETD4_S1 || a.mode == Z_EULER;
-    const bool reuse = stage1 && !ctrl->fresh;  // retry of a rejected step: N_u / R-hat unchanged
+    const bool reuse = stage1 && !c_fresh;  // retry of a rejected step: N_u / R-hat unchanged
     const bool need_fwd = (a.mode <= Z_EULER && !reuse) || a.mode == Z_FWD_PLAIN;
 
     if (need_fwd) {
@@ -163,8 +169,8 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
         const void* srcB = I.B;
         if constexpr (sizeof(T) == 4) {
             if (stage1) {
-                srcA = I.G[ctrl->ab_state][0];
-                srcB = I.G[ctrl->ab_state][1];
+                srcA = c_ab ? g_a[1] : g_a[0];
+                srcB = c_ab ? g_b[1] : g_b[0];
             }
         }
         const C* gA = reinterpret_cast<const C*>(a.mode == Z_FWD_PLAIN ? a.cin : srcA);
