@@ -117,10 +117,13 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     const int z = blockIdx.x;
     const int tid = threadIdx.x;
     if (z >= p.nz) return;
+    // the control fields in one batch of independent loads, so the CTA does not wait on a
+    // chain of dependent loads before its data moves
+    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_part = ctrl->part_state, c_u = ctrl->u_state;
     const bool stepping = a.mode <= XY_FUSED;
     if (stepping) {
-        if (ctrl->done) return;
-        if (a.skip_if_stale && !ctrl->fresh) return;
+        if (c_done) return;
+        if (a.skip_if_stale && !c_fresh) return;
     }
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
     C* twM = S + NY * pitch;                // W_M^m
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         if (a.mode == XY_INV_PLAIN) {
             P0 = reinterpret_cast<const C*>(a.cin) + (size_t)z * plane;
         } else {
-            const int set = part_set(ctrl, a.role);
+            const int set = a.role == R_WORK ? 2 : (a.role == R_STATE ? c_part : 1 - c_part);  // part_set
             P0 = reinterpret_cast<const C*>(I.P[set][0]) + (size_t)z * plane;
             P2 = reinterpret_cast<const C*>(I.P[set][1]) + (size_t)z * plane;
         }
@@ -296,8 +299,8 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             PSum<T> ag, ah;
             if constexpr (sizeof(T) == 4) {
                 // u = U[u_state] + (u - u_state); the candidate pass keeps its u for the next state
-                const float4* Us = reinterpret_cast<const float4*>(I.U[ctrl->u_state]) + (size_t)z * NY * M;
-                float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - ctrl->u_state]) + (size_t)z * NY * M
+                const float4* Us = reinterpret_cast<const float4*>(I.U[c_u]) + (size_t)z * NY * M;
+                float4* Uo = a.role == R_CAND ? reinterpret_cast<float4*>(I.U[1 - c_u]) + (size_t)z * NY * M
                                               : nullptr;
                 Acc2 as2, af2;
                 PSum2 ag2, ah2;
