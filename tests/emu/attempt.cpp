@@ -1,13 +1,13 @@
-// Test infrastructure (tests/test_kernel_emulation.py): one FP32-form ETD-RK2 attempt
-// on an n x n x nz grid through the library's own kernel sources, run on the host by the CUDA
-// emulation in fake/ and checked by AddressSanitizer.  Every device buffer and every
+// Test infrastructure (tests/test_kernel_emulation.py): one FP32-form attempt (ETD-RK2,
+// ETD-RK4 or Euler) on an n x n x nz grid through the library's own kernel sources, run
+// on the host by the CUDA emulation in fake/ and checked by AddressSanitizer.  Every device buffer and every
 // block's shared memory is a separate heap allocation of the exact size the library
 // gives it, so an index one element past any of them is reported.
 //
 // Sequence (as cb_set_phi and one attempt of the stepper's loop run it):
 //   z Z_INV_STATE (state)   -> xy XY_FUSED (state)
-//   prologue + coefficient fill -> z S1 -> xy FUSED (work) -> z S2 -> xy FUSED (candidate)
-//   -> decide
+//   prologue + coefficient fill -> the method's z stages, each but the last followed by
+//   xy FUSED (work) -> xy FUSED (candidate) -> decide
 // The xy passes run on the schedule given on the command line: 2 = one CTA per plane,
 // 3 = two-CTA clusters.  The sums the passes leave are printed for comparison.
 #include <cstdio>
@@ -112,7 +112,7 @@ static void* zalloc(size_t b) {
 
 // the Params fields make_params (stepper.cuh) sets for an FP32-form ETD-RK2 handle
 // of n x n x nz with epssize 3 (eps = 1.5 h), M1 = M2 = 1e4 and the adaptive schedule
-static Params params(int n, int nz) {
+static Params params(int n, int nz, int method) {
     Params p;
     memset(&p, 0, sizeof p);
     p.nx = p.ny = n;
@@ -128,17 +128,18 @@ static Params params(int n, int nz) {
     p.ga = 1;
     p.M1 = 1e4;
     p.M2 = 1e4;
-    p.method = M_ETD2;
+    p.method = method;
     p.adaptive = 1;
     p.etd4_ref = 1;
     p.kmax = 2 * (n / 2) * (n / 2) + (nz / 2) * (nz / 2);
     p.grow_every = 4;
-    p.grow_factor = 2;
-    p.dt_cap = 1e-3;
-    p.cap_probe = 1.4;
+    const bool euler = method == M_EULER;
+    p.grow_factor = euler ? 1.4 : 2;
+    p.dt_cap = euler ? 1e300 : 1e-3;
+    p.cap_probe = euler ? 0.0 : 1.4;
     p.dt_min = 1e-23;
     p.tmax = 4;
-    const double beta = -p.eta / p.eps;
+    const double beta = euler ? p.eta : -p.eta / p.eps;
     p.d_ieps = 1 / p.eps;
     p.d_ieps2 = 1 / (p.eps * p.eps);
     p.d_ieps3 = p.d_ieps2 * p.d_ieps;
@@ -159,9 +160,9 @@ static Params params(int n, int nz) {
     return p;
 }
 
-template <int N, int NZ> int run(int path) {
+template <int N, int NZ> int run(int path, int method) {
     using T = float;
-    const Params p = params(N, NZ);
+    const Params p = params(N, NZ, method);
     const size_t ns = (size_t)NZ * N * p.nc;
     const int ntiles = (int)((N * p.nc + 15) / 16);
     InstT<T> h;
@@ -169,6 +170,10 @@ template <int N, int NZ> int run(int path) {
     for (int i = 0; i < 2; ++i) h.spec[i] = zalloc(ns * 16);
     h.ahat = zalloc(ns * 16);
     h.Nu = zalloc(ns * 8);
+    if (method == M_ETD4) {  // the stepper holds N-hat_a, N-hat_b for ETD-RK4 only
+        h.Na = zalloc(ns * 8);
+        h.Nb = zalloc(ns * 8);
+    }
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 2; ++j) h.P[i][j] = zalloc(ns * 8);
     h.A = zalloc(ns * 8);
@@ -227,13 +232,27 @@ template <int N, int NZ> int run(int path) {
     };
     using GP = std::integral_constant<int, ZG_PLAIN>;
     using G2 = std::integral_constant<int, ZG_ETD2>;
+    using G4 = std::integral_constant<int, ZG_ETD4>;
+    using GE = std::integral_constant<int, ZG_EULER>;
     z(Z_INV_STATE, R_STATE, GP{});
     xy(XY_FUSED, R_STATE);
     c.E_state = c.sc[R_STATE].E;
     emu::launch(dim3(64, 1), 256, 0, 1, [&] { prologue_fill_kernel<T>(d, 1, 0); });
-    z(Z_ETD2_S1, R_WORK, G2{});
-    xy(XY_FUSED, R_WORK);
-    z(Z_ETD2_S2, R_CAND, G2{});
+    if (method == M_ETD2) {
+        z(Z_ETD2_S1, R_WORK, G2{});
+        xy(XY_FUSED, R_WORK);
+        z(Z_ETD2_S2, R_CAND, G2{});
+    } else if (method == M_ETD4) {
+        z(Z_ETD4_S1, R_WORK, G4{});
+        xy(XY_FUSED, R_WORK);
+        z(Z_ETD4_S2, R_WORK, G4{});
+        xy(XY_FUSED, R_WORK);
+        z(Z_ETD4_S3, R_WORK, G4{});
+        xy(XY_FUSED, R_WORK);
+        z(Z_ETD4_S4, R_CAND, G4{});
+    } else {
+        z(Z_EULER, R_CAND, GE{});
+    }
     xy(XY_FUSED, R_CAND);
     emu::launch(dim3(1), 128, 0, 1, [&] { decide_kernel<T>(d, 1, 0); });
     printf("state V %.17g S %.17g E %.17g sum_g %.17g\n", c.sc[R_STATE].V, c.sc[R_STATE].S, c.sc[R_STATE].E,
@@ -251,11 +270,12 @@ int main(int argc, char** argv) {
     const int n = argc > 1 ? atoi(argv[1]) : 32;
     const int nz = argc > 2 ? atoi(argv[2]) : n;
     const int path = argc > 3 ? atoi(argv[3]) : XYP_SINGLE;
-    if (n == 16 && nz == 16) return run<16, 16>(path);
-    if (n == 32 && nz == 32) return run<32, 32>(path);
-    if (n == 48 && nz == 16) return run<48, 16>(path);
-    if (n == 64 && nz == 16) return run<64, 16>(path);
-    if (n == 96 && nz == 16) return run<96, 16>(path);
+    const int method = argc > 4 ? atoi(argv[4]) : M_ETD2;
+    if (n == 16 && nz == 16) return run<16, 16>(path, method);
+    if (n == 32 && nz == 32) return run<32, 32>(path, method);
+    if (n == 48 && nz == 16) return run<48, 16>(path, method);
+    if (n == 64 && nz == 16) return run<64, 16>(path, method);
+    if (n == 96 && nz == 16) return run<96, 16>(path, method);
     fprintf(stderr, "grid %dx%dx%d not built into the emulation harness\n", n, n, nz);
     return 2;
 }

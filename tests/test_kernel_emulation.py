@@ -3,8 +3,9 @@
 The kernel headers of cudabubble_gb300/csrc are compiled for the host against a
 CUDA emulation (tests/emu/fake: one OS thread per CUDA thread, real barriers for
 __syncthreads, warp shuffles and cluster barriers) with AddressSanitizer, and one
-FP32-form ETD-RK2 attempt (set-up pass, prologue, coefficient fill, z S1, fused xy
-pass, z S2, fused xy pass, decide) runs on both xy schedules.  Every device buffer
+FP32-form attempt (set-up pass, prologue and coefficient fill, the method's z stages
+with their fused xy passes, decide) runs: ETD-RK2 on both xy schedules, ETD-RK4 and
+Euler on the one-CTA schedule.  Every device buffer
 and every block's shared memory is an exact-size heap allocation, so any access
 outside them fails the test.  The two schedules must also leave the same sums.
 Needs g++ with AddressSanitizer; no GPU."""
@@ -42,9 +43,13 @@ def harness(tmp_path_factory):
     return str(exe)
 
 
-def run_attempt(exe, n, nz, path):
+METHODS = {"euler": 0, "etd2": 1, "etd4": 2}
+
+
+def run_attempt(exe, n, nz, path, method="etd2"):
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1")
-    r = subprocess.run([exe, str(n), str(nz), str(path)], capture_output=True, text=True, env=env, timeout=900)
+    r = subprocess.run([exe, str(n), str(nz), str(path), str(METHODS[method])], capture_output=True, text=True,
+                       env=env, timeout=900)
     assert "AddressSanitizer" not in r.stderr, r.stderr[-6000:]
     assert r.returncode == 0, r.stderr[-3000:]
     vals = {}
@@ -55,13 +60,18 @@ def run_attempt(exe, n, nz, path):
     return vals
 
 
-@pytest.mark.parametrize("n,nz", [(16, 16), (32, 32), (48, 16)])
-def test_single_cta_schedule_in_bounds(harness, n, nz):
-    v = run_attempt(harness, n, nz, 2)
+@pytest.mark.parametrize("n,nz,method", [(16, 16, "etd2"), (32, 32, "etd2"), (48, 16, "etd2"), (32, 32, "etd4"),
+                                          (32, 32, "euler")])
+def test_single_cta_schedule_in_bounds(harness, n, nz, method):
+    v = run_attempt(harness, n, nz, 2, method)
     assert v["ctrl.attempts"] == 1
     # every last-CTA counter was reset by the CTA that finalised
     assert all(v[f"ctrl.{k}"] == 0 for k in ("cnt_xy", "cnt_z"))
-    assert all(abs(v[k]) < float("inf") for k in ("state.V", "state.S", "cand.V", "cand.S"))
+    # the synthetic state (a real-space field that does not match its spectrum) keeps the
+    # ETD-RK2 candidate finite; the other methods' candidates may overflow in FP32, and
+    # decide copies an accepted candidate into the state
+    if method == "etd2":
+        assert all(abs(v[k]) < float("inf") for k in ("state.V", "state.S", "cand.V", "cand.S"))
 
 
 @pytest.mark.parametrize("n", [64])
