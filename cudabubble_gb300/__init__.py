@@ -2,6 +2,5 @@
 phase-field elastic bending energy.  The compute path is libcbstep.so
 (``include/cbstep.h``); this package is its Python face."""
 from . import capi, shapes  # noqa: F401
-from .belastic import Belastic  # noqa: F401
 
-__all__ = ["capi", "shapes", "Belastic"]
+__all__ = ["capi", "shapes"]

@@ -22,7 +22,7 @@ CB_FP64, CB_FP32 = 0, 1
  CB_FIELD_DZ, CB_FIELD_S, CB_FIELD_NLD_HAT, CB_FIELD_RHS) = range(12)
 XYP_AUTO, XYP_SPLIT, XYP_SINGLE, XYP_CLUSTER = range(4)
 (CB_RUNNING, CB_DONE_TARGET, CB_DONE_DT_UNDERFLOW, CB_DONE_SMALL_ENERGY, CB_DONE_NONFINITE, CB_DONE_CONVERGED,
- CB_DONE_TMAX) = range(7)
+ CB_DONE_TMAX, CB_DONE_CANCELLED) = range(8)
 STATUS_NAMES = {0: "running", 1: "target", 2: "dt_underflow", 3: "small_energy", 4: "nonfinite", 5: "converged",
                 6: "tmax"}
 ERROR_NAMES = {CB_EINVAL: "CB_EINVAL", CB_ENOMEM: "CB_ENOMEM", CB_ECUDA: "CB_ECUDA", CB_ENONFINITE: "CB_ENONFINITE",
@@ -65,7 +65,7 @@ class cb_tune_result(C.Structure):
 class cb_request(C.Structure):
     _fields_ = [("params", cb_params), ("axes", C.c_double * 3), ("centre", C.c_double * 3),
                 ("axes2", C.c_double * 3), ("centre2", C.c_double * 3), ("arrival_s", C.c_double),
-                ("max_steps", C.c_int), ("pad", C.c_int)]
+                ("max_steps", C.c_int), ("cancel_ms", C.c_int)]
 
 
 class cb_result(C.Structure):
@@ -104,6 +104,7 @@ SIGNATURES = {
     "cb_shape_adjust": (C.c_int, [C.c_void_p, C.c_int, _P(cb_adjust_stats)]),
     "cb_autotune": (C.c_int, [C.c_void_p, C.c_int, _P(cb_tune_result)]),
     "cb_synchronize": (C.c_int, [C.c_void_p]),
+    "cb_set_launch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "cb_handle_bytes": (C.c_longlong, [C.c_void_p]),
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
     "cb_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
@@ -285,6 +286,11 @@ class Stepper:
         cnt = (C.c_int * len(self.KERNEL_KINDS))()
         check(lib().cb_profile_kernels(self.h, nattempts, flush_bytes, ms, cnt))
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.KERNEL_KINDS)}
+
+    def set_launch_limit(self, n: int):
+        """Bound the attempts one run / run_timed / shape_adjust call may launch (0: none);
+        a call that reaches it raises CB_ETIMEOUT and leaves the state at its last accepted step."""
+        check(lib().cb_set_launch_limit(self.h, C.c_longlong(n)))
 
     def nbytes(self) -> int:
         return int(lib().cb_handle_bytes(self.h))

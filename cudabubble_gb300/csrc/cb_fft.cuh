@@ -18,6 +18,22 @@
 
 namespace cb {
 
+// ------------------------------------------- programmatic dependent launch
+// The stepper's kernels are launched with programmatic stream serialisation, so a
+// kernel's CTAs are scheduled while the previous kernel in the stream still runs.
+// Each kernel lets its successor launch at once (CB_PDL_TRIGGER) and, before it reads
+// anything an earlier kernel wrote, waits for the previous grid to complete with its
+// memory visible (CB_PDL_WAIT).  Work before the wait may touch only what no kernel
+// of the stream writes (twiddle tables, instance descriptors).  Without a programmatic
+// predecessor the wait returns at once.
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+#define CB_PDL_TRIGGER() asm volatile("griddepcontrol.launch_dependents;" ::: "memory")
+#define CB_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+#else
+#define CB_PDL_TRIGGER() ((void)0)
+#define CB_PDL_WAIT() ((void)0)
+#endif
+
 // ---------------------------------------------------------------- complex
 template <class T> struct CT;
 template <> struct CT<float> { using type = float2; };

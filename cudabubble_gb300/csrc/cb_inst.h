@@ -130,7 +130,7 @@ template <> struct PC<double> {
 enum { SCHED_LOOP = 0, SCHED_SHAPE = 1 };
 
 enum { ST_RUNNING = 0, ST_TARGET = 1, ST_DT_UNDERFLOW = 2, ST_SMALL_ENERGY = 3, ST_NONFINITE = 4, ST_CONVERGED = 5,
-       ST_TMAX = 6 };
+       ST_TMAX = 6, ST_CANCELLED = 7 };
 
 template <class T> struct InstT {
     void* spec[2];  // phi-hat state / candidate (swap via ctrl->spec_state)

@@ -14,6 +14,31 @@ namespace cb {
 
 constexpr size_t kMaxSmem = 227 * 1024;
 
+// Launch with programmatic stream serialisation: the kernel's CTAs may be scheduled
+// while the previous kernel in the stream still runs, and wait in CB_PDL_WAIT for its
+// results (cb_fft.cuh).  Captured into a graph, the launch becomes a programmatic edge.
+// A build with -DCB_NO_PDL launches with plain stream order.
+template <class... KArgs, class... Args>
+static cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                            Args... args) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+#ifndef CB_NO_PDL
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+#else
+    (void)at;
+#endif
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // threads of the single-CTA xy pass for planes of 96^2 and 128^2: the
 // nonlinear pass (two fields both ways) gains from 32 warps per plane, the
 // reductions (inverse only) do not (build-time knobs, measured on GB300)
@@ -49,8 +74,7 @@ static cudaError_t xyc_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs&
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    xyc_fused_kernel<T, NX, NT><<<dim3(2 * nzmax, ninst), NT, sm, s>>>(d, a);
-    return cudaGetLastError();
+    return launch_k(xyc_fused_kernel<T, NX, NT>, dim3(2 * nzmax, ninst), dim3(NT), sm, s, d, a);
 }
 
 template <class T, int NX, int NF, int NT>
@@ -62,8 +86,7 @@ static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArg
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    xy_kernel<T, NX, NT, NF><<<dim3(nzmax, ninst), NT, xy_smem_bytes<T, NX>(NF), s>>>(d, a);
-    return cudaGetLastError();
+    return launch_k(xy_kernel<T, NX, NT, NF>, dim3(nzmax, ninst), dim3(NT), xy_smem_bytes<T, NX>(NF), s, d, a);
 }
 
 template <class T, int NX>
@@ -101,8 +124,7 @@ static cudaError_t ycol_go(const InstT<T>* d, int ninst, int nzmax, const YArgs&
         attr = true;
     }
     const int ntx = (NY / 2 + 1 + TX - 1) / TX;  // square planes: nc = NY/2 + 1
-    ycol_kernel<T, NY, TX, NT><<<dim3(nzmax * ntx, ninst), NT, sm, s>>>(d, a);
-    return cudaGetLastError();
+    return launch_k(ycol_kernel<T, NY, TX, NT>, dim3(nzmax * ntx, ninst), dim3(NT), sm, s, d, a);
 }
 
 template <class T, int NX>
@@ -116,8 +138,7 @@ static cudaError_t xrow_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    xrow_kernel<T, NX, RPC, NT><<<dim3(nzmax * NX / RPC, ninst), NT, sm, s>>>(d, a);
-    return cudaGetLastError();
+    return launch_k(xrow_kernel<T, NX, RPC, NT>, dim3(nzmax * NX / RPC, ninst), dim3(NT), sm, s, d, a);
 }
 
 // one xy mode as y pass(es) around the x-row pass
@@ -173,8 +194,7 @@ static cudaError_t z_go_g(const InstT<T>* d, int ninst, int ntiles, const ZArgs&
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    z_kernel<T, NZ, TX, NT, MG><<<dim3(ntiles, ninst), NT, sm, s>>>(d, a);
-    return cudaGetLastError();
+    return launch_k(z_kernel<T, NZ, TX, NT, MG>, dim3(ntiles, ninst), dim3(NT), sm, s, d, a);
 }
 
 template <class T, int NZ>
@@ -268,12 +288,10 @@ cudaError_t Launch<T>::z(int nz, const InstT<T>* d, int ninst, int ntiles, const
     }
 }
 template <class T> cudaError_t Launch<T>::decide(const InstT<T>* d, int ninst, int raw, cudaStream_t s) {
-    decide_kernel<T><<<(ninst + 127) / 128, 128, 0, s>>>(d, ninst, raw);
-    return cudaGetLastError();
+    return launch_k(decide_kernel<T>, dim3((ninst + 127) / 128), dim3(128), 0, s, d, ninst, raw);
 }
 template <class T> cudaError_t Launch<T>::coef(const InstT<T>* d, int ninst, int accurate, cudaStream_t s, int raw) {
-    prologue_fill_kernel<T><<<dim3(64, ninst), 256, 0, s>>>(d, accurate, raw);
-    return cudaGetLastError();
+    return launch_k(prologue_fill_kernel<T>, dim3(64, ninst), dim3(256), 0, s, d, accurate, raw);
 }
 template <class T> cudaError_t Launch<T>::to_double(const void* in, double* out, size_t n, cudaStream_t s) {
     const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);

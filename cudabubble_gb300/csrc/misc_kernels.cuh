@@ -204,6 +204,8 @@ __device__ inline void fill_table(const InstT<T>& I, const Params& p, int slot, 
 // the old state before it counts itself done, so none sees a half-written one.
 template <class T>
 __global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int accurate, int raw) {
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
     const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
@@ -332,6 +334,8 @@ __device__ inline void decide_update(Ctrl* c, const Params& p, int raw) {
 // kernel's length.
 template <class T>
 __global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const InstT<T>& I = insts[i];

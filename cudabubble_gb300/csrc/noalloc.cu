@@ -70,24 +70,27 @@ intf_noalloc_kernel(const double* __restrict__ u, int nz, long long plane, doubl
 std::mutex g_noalloc_mu;
 NoAllocScratch* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-// Set-up, once per device with that device current: resolve the scratch
-// address and clear its counter.  Synchronous, so the first call for a device
-// must not be made while a stream is being captured.
+// The scratch address of the current device, resolved on every call (it does not
+// allocate): a cached address goes stale when the device's context is rebuilt
+// (cudaDeviceReset, a new primary context).  The first call that sees an address
+// for a device -- once per device and context -- clears the counter
+// synchronously, so that first call must not be made while a stream is being
+// captured.
 int noalloc_scratch(NoAllocScratch** out) {
     int dev = 0;
     CB_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices)
         return fail(CB_EINVAL, "cb_intf_noalloc: device %d beyond the %d supported", dev, kNoAllocMaxDevices);
+    void* p = nullptr;
+    CB_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    NoAllocScratch* s = static_cast<NoAllocScratch*>(p);
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        CB_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        NoAllocScratch* s = static_cast<NoAllocScratch*>(p);
+    if (g_noalloc_ptr[dev] != s) {
         CB_CK(cudaMemset(&s->count, 0, sizeof(unsigned)));
         CB_CK(cudaDeviceSynchronize());
         g_noalloc_ptr[dev] = s;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = s;
     return CB_OK;
 }
 

@@ -14,6 +14,8 @@
 // or served mode; these are additions of this implementation.
 #include <chrono>
 #include <deque>
+#include <iterator>
+#include <map>
 #include <thread>
 
 #include "stepper.cuh"
@@ -361,135 +363,410 @@ template <class T> class Batch final : public BatchBase {
 };
 
 // ---------------------------------------------------------------- server
-template <class T>
-static int make_phi0(Stepper<T>& s, const cb_request& r, double* stage) {
-    const Params& p = s.params();
-    const double L = (r.params.lenx > 0 ? r.params.lenx : 1.0) * kTwoPi;
-    ellipsoid_kernel<<<1024, 256>>>(stage, p.nx, p.nz, L, p.eps, r.axes[0], r.axes[1], r.axes[2], r.centre[0],
-                                    r.centre[1], r.centre[2], r.axes2[0], r.axes2[1], r.axes2[2], r.centre2[0],
-                                    r.centre2[1], r.centre2[2]);
-    CB_CK(cudaGetLastError());
-    CB_CK(cudaDeviceSynchronize());
-    return s.set_phi(stage, true);
-}
+// Device memory of the served pool: one region reserved before the trace starts,
+// carved into instance arenas first-fit, with freed blocks merged with their free
+// neighbours, so admitting a request allocates nothing from the driver.
+class ArenaRegion {
+   public:
+    ~ArenaRegion() { cudaFree(base); }
+    int init(size_t bytes) {
+        size = bytes & ~(size_t)255;
+        if (cudaMalloc(&base, size) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(CB_ENOMEM, "served pool: cudaMalloc of its %zu-byte region failed", size);
+        }
+        free_[0] = size;
+        return CB_OK;
+    }
+    void* take(size_t n) {
+        n = (n + 255) & ~(size_t)255;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < n) continue;
+            const size_t off = it->first, len = it->second;
+            free_.erase(it);
+            if (len > n) free_[off + n] = len - n;
+            return static_cast<char*>(base) + off;
+        }
+        return nullptr;
+    }
+    void give(void* ptr, size_t n) {
+        n = (n + 255) & ~(size_t)255;
+        size_t off = static_cast<size_t>(static_cast<char*>(ptr) - static_cast<char*>(base));
+        auto nx = free_.lower_bound(off);
+        if (nx != free_.end() && off + n == nx->first) {  // merge with the block after
+            n += nx->second;
+            nx = free_.erase(nx);
+        }
+        if (nx != free_.begin()) {  // and with the block before
+            auto pv = std::prev(nx);
+            if (pv->first + pv->second == off) {
+                pv->second += n;
+                return;
+            }
+        }
+        free_[off] = n;
+    }
+    size_t bytes() const { return size; }
+
+   private:
+    void* base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> length
+};
+
+// One size class of the server: its slot table, its own attempt graph and stream,
+// so each class advances at its own pace (a 32^3 request is not paced by a 256^3
+// one), and its per-slot summaries copied back to pinned host memory.
+template <class T> struct ServeClass {
+    int nx = 0, nz = 0, method = 0, accurate = 0, split = 0, cap = 0, ntiles = 0, quantum = 1;
+    long long bytes = 0;
+    InstT<T>* table = nullptr;   // device slot table
+    InstT<T>* h_table = nullptr; // pinned mirror, the source of the table's copies
+    SlotSummary* d_sum = nullptr;
+    SlotSummary* h_sum = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaGraphExec_t g = nullptr;
+    std::vector<int> slot_act;  // index into the active list, -1 for a free slot
+    int active = 0;
+    bool inflight = false;
+};
 
 template <class T> struct Active {
     std::unique_ptr<Stepper<T>> st;
-    int req, cls, slot;
-    long long bytes;
+    void* mem = nullptr;
+    int req = -1, cls = -1, slot = -1;
+    long long bytes = 0;
+    double cancel_at = 0.0;  // > 0: trace time at which the request is cancelled
 };
 
-// Continuous batching over an arrival trace, in real time: arrivals join a
-// FIFO queue; the head is admitted while its class has a free slot and the
-// HBM budget holds its instance; every loop iteration runs `quantum`
-// attempts of all admitted instances; finished ones are retired at once.
+template <class T> struct Server {
+    std::vector<ServeClass<T>> cls;
+    ArenaRegion region;
+    cudaStream_t adm = nullptr;  // admission / retirement stream (set-up of admitted instances)
+    Ctrl* dummy_ctrl = nullptr;
+    InstT<T> dummy{};
+    double* stage = nullptr;     // phi0 of an admitted request
+
+    ~Server() {
+        for (auto& c : cls) {
+            if (c.s) cudaStreamSynchronize(c.s);
+            if (c.g) cudaGraphExecDestroy(c.g);
+            cudaFree(c.table);
+            cudaFree(c.d_sum);
+            cudaFreeHost(c.h_table);
+            cudaFreeHost(c.h_sum);
+            if (c.ev) cudaEventDestroy(c.ev);
+            if (c.s) cudaStreamDestroy(c.s);
+        }
+        if (adm) cudaStreamSynchronize(adm);
+        cudaFree(dummy_ctrl);
+        cudaFree(stage);
+        if (adm) cudaStreamDestroy(adm);
+    }
+
+    int find(const Eff& e) const {
+        for (size_t i = 0; i < cls.size(); ++i) {
+            const auto& c = cls[i];
+            if (c.nx == e.p.nx && c.nz == e.p.nz && c.method == e.p.method && c.accurate == e.accurate &&
+                c.split == e.p.split)
+                return (int)i;
+        }
+        return -1;
+    }
+
+    // classes, their graphs and every allocation of the trace, before it starts
+    int setup(const cb_request* reqs, int n, long long budget, int max_slots, int quantum) {
+        CB_CK(cudaStreamCreateWithFlags(&adm, cudaStreamNonBlocking));
+        CB_CK(cudaMalloc(&dummy_ctrl, sizeof(Ctrl)));
+        Ctrl dc;
+        memset(&dc, 0, sizeof dc);
+        dc.done = 1;
+        CB_CK(cudaMemcpy(dummy_ctrl, &dc, sizeof dc, cudaMemcpyHostToDevice));
+        memset(&dummy, 0, sizeof dummy);
+        dummy.ctrl = dummy_ctrl;
+        long long maxN = 0;
+        for (int i = 0; i < n; ++i) {
+            Eff e;
+            int rc = make_params(reqs[i].params, e);
+            if (rc) return rc;
+            if (!Launch<T>::xy_supported(e.p.nx) || !Launch<T>::z_supported(e.p.nz))
+                return fail(CB_EUNSUPPORTED, "request %d: grid %d^2x%d not built", i, e.p.nx, e.p.nz);
+            maxN = std::max<long long>(maxN, e.p.N);
+            if (find(e) >= 0) continue;
+            ServeClass<T> c;
+            c.nx = e.p.nx; c.nz = e.p.nz; c.method = e.p.method; c.accurate = e.accurate; c.split = e.p.split;
+            c.bytes = (long long)instance_arena_bytes<T>(e.p);
+            if (c.bytes > budget) return fail(CB_ENOMEM, "request %d needs %lld bytes, over the budget", i, c.bytes);
+            c.cap = (int)std::max<long long>(1, std::min<long long>(max_slots, budget / c.bytes));
+            const int tx = Launch<T>::z_tile();
+            c.ntiles = (e.p.ny * e.p.nc + tx - 1) / tx;
+            // attempts per launch batch: more for small grids, whose attempts are short
+            // next to a host round trip
+            const double vol = (double)e.p.N / (128.0 * 128.0 * 128.0);
+            c.quantum = (int)std::min(32.0 * quantum, std::max((double)quantum, quantum / std::max(vol, 1e-9)));
+            c.slot_act.assign(c.cap, -1);
+            CB_CK(cudaMalloc(&c.table, sizeof(InstT<T>) * c.cap));
+            CB_CK(cudaMalloc(&c.d_sum, sizeof(SlotSummary) * c.cap));
+            CB_CK(cudaMallocHost(&c.h_table, sizeof(InstT<T>) * c.cap));
+            CB_CK(cudaMallocHost(&c.h_sum, sizeof(SlotSummary) * c.cap));
+            for (int k = 0; k < c.cap; ++k) c.h_table[k] = dummy;
+            CB_CK(cudaMemcpy(c.table, c.h_table, sizeof(InstT<T>) * c.cap, cudaMemcpyHostToDevice));
+            CB_CK(cudaEventCreateWithFlags(&c.ev, cudaEventDisableTiming));
+            // the twiddle tables of the class, made (and cached) now rather than at admission
+            cudaError_t te = cudaSuccess;
+            if (!twiddle_table<T>(e.p.nx, 1, &te) || !twiddle_table<T>(e.p.ny, 0, &te) ||
+                !twiddle_table<T>(e.p.nz, 0, &te))
+                return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(te));
+            if (sizeof(T) == 4 && (!twiddle_table<double>(e.p.nx, 1, &te) || !twiddle_table<double>(e.p.ny, 0, &te) ||
+                                   !twiddle_table<double>(e.p.nz, 0, &te)))
+                return fail(CB_ECUDA, "twiddles: %s", cudaGetErrorString(te));
+            cls.push_back(c);
+        }
+        // Stream priorities by grid size: the device hands free SMs to the CTAs of the
+        // smaller grids first, so their short attempts are not queued behind the large
+        // grids' long launches (shortest job first across classes).
+        int lo = 0, hi = 0;
+        CB_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        std::vector<long long> sizes;
+        for (auto& c : cls) sizes.push_back((long long)c.nx * c.nx * c.nz);
+        std::sort(sizes.begin(), sizes.end());
+        sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+        const int levels = lo - hi + 1;  // hi is the numerically smallest (greatest) priority
+        for (auto& c : cls) {
+            const long long sz = (long long)c.nx * c.nx * c.nz;
+            const int rank = (int)(std::lower_bound(sizes.begin(), sizes.end(), sz) - sizes.begin());
+            const int pri = hi + (int)((long long)rank * levels / (long long)sizes.size());
+            CB_CK(cudaStreamCreateWithPriority(&c.s, cudaStreamNonBlocking, std::min(pri, lo)));
+            cudaGraph_t gr = nullptr;
+            CB_CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
+            cudaError_t r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false,
+                                             c.split, c.s);
+            cudaError_t ee = cudaStreamEndCapture(c.s, &gr);
+            if (r != cudaSuccess || ee != cudaSuccess) {
+                if (gr) cudaGraphDestroy(gr);
+                return fail(CB_ECUDA, "class capture: %s", cudaGetErrorString(r != cudaSuccess ? r : ee));
+            }
+            cudaError_t ie = cudaGraphInstantiate(&c.g, gr, 0);
+            cudaGraphDestroy(gr);
+            CB_CK(ie);
+        }
+        size_t fr = 0, tot = 0;
+        CB_CK(cudaMemGetInfo(&fr, &tot));
+        const size_t margin = (size_t)2 << 30;
+        size_t want = (size_t)budget;
+        if (fr > margin) want = std::min(want, fr - margin);
+        int rc = region.init(want);
+        if (rc) return rc;
+        for (auto& c : cls)
+            if ((size_t)c.bytes > region.bytes())
+                return fail(CB_ENOMEM, "a %d^2x%d instance needs %lld bytes, more than the %zu the device can reserve",
+                            c.nx, c.nz, c.bytes, region.bytes());
+        CB_CK(cudaMalloc(&stage, (size_t)maxN * sizeof(double)));
+        return CB_OK;
+    }
+
+    // set up request r in a free slot of class ci on caller-owned memory; false when the
+    // region has no block for it right now
+    int admit(const cb_request& r, int ci, Active<T>& a, bool* placed) {
+        ServeClass<T>& c = cls[ci];
+        *placed = false;
+        void* mem = region.take((size_t)c.bytes);
+        if (!mem) return CB_OK;
+        a.mem = mem;
+        a.bytes = c.bytes;
+        a.st.reset(new Stepper<T>());
+        int rc = a.st->init_in(r.params, mem, adm);
+        if (rc) return rc;
+        const Params& p = a.st->params();
+        const double L = (r.params.lenx > 0 ? r.params.lenx : 1.0) * kTwoPi;
+        ellipsoid_kernel<<<1024, 256, 0, adm>>>(stage, p.nx, p.nz, L, p.eps, r.axes[0], r.axes[1], r.axes[2],
+                                                r.centre[0], r.centre[1], r.centre[2], r.axes2[0], r.axes2[1],
+                                                r.axes2[2], r.centre2[0], r.centre2[1], r.centre2[2]);
+        CB_CK(cudaGetLastError());
+        rc = a.st->set_phi(stage, true);  // ordered after the kernel on the same stream; synchronises it
+        if (rc) return rc;
+        rc = a.st->prepare_run(r.max_steps > 0 ? r.max_steps : INT_MAX / 2);
+        if (rc) return rc;
+        int k = 0;
+        while (c.slot_act[k] >= 0) ++k;
+        a.cls = ci;
+        a.slot = k;
+        c.h_table[k] = a.st->inst();
+        // stream-ordered on the class stream: the slot changes between two of its batches
+        CB_CK(cudaMemcpyAsync(c.table + k, c.h_table + k, sizeof(InstT<T>), cudaMemcpyHostToDevice, c.s));
+        *placed = true;
+        return CB_OK;
+    }
+
+    // empty the slot (stream-ordered) and give the arena back; the class is idle
+    int retire(Active<T>& a) {
+        ServeClass<T>& c = cls[a.cls];
+        c.h_table[a.slot] = dummy;
+        CB_CK(cudaMemcpyAsync(c.table + a.slot, c.h_table + a.slot, sizeof(InstT<T>), cudaMemcpyHostToDevice, c.s));
+        CB_CK(cudaStreamSynchronize(c.s));
+        c.slot_act[a.slot] = -1;
+        c.active--;
+        a.st.reset();  // synchronises the admission stream; the arena stays the region's
+        region.give(a.mem, (size_t)a.bytes);
+        a.mem = nullptr;
+        return CB_OK;
+    }
+
+    int launch(ServeClass<T>& c) {
+        for (int i = 0; i < c.quantum; ++i) CB_CK(cudaGraphLaunch(c.g, c.s));
+        gather_kernel<T><<<(c.cap + 127) / 128, 128, 0, c.s>>>(c.table, c.cap, c.d_sum);
+        CB_CK(cudaGetLastError());
+        CB_CK(cudaMemcpyAsync(c.h_sum, c.d_sum, sizeof(SlotSummary) * c.cap, cudaMemcpyDeviceToHost, c.s));
+        CB_CK(cudaEventRecord(c.ev, c.s));
+        c.inflight = true;
+        return CB_OK;
+    }
+};
+
+// Continuous batching over an arrival trace, in real time.  Arrivals join a queue;
+// every pass admits, in arrival order, each queued request whose size class has a
+// free slot (a request whose class is full is passed over, not waited on) while the
+// HBM budget and the pool's region hold its instance; a request the budget cannot
+// hold stops admission behind it, so large requests are not starved.  Each class
+// runs batches of attempts on its own stream; a class whose batch has finished
+// retires its finished (or cancelled) requests, takes new ones, and starts its next
+// batch at once.  A request with cancel_ms > 0 is cancelled that long after its
+// arrival: dropped from the queue, or retired from its slot after its class's
+// current batch, with CB_DONE_CANCELLED and its memory returned.
 template <class T>
 static int serve_impl(const cb_request* reqs, int n, long long budget, int max_slots, int quantum, cb_result* res,
                       double** phi_out, cb_serve_stats* stats) {
-    Pool<T> pool;
-    int rc = pool.init();
+    Server<T> sv;
+    int rc = sv.setup(reqs, n, budget, max_slots, quantum);
     if (rc) return rc;
-    for (int i = 0; i < n; ++i) {  // size classes of the trace
+    std::vector<int> rcls(n);
+    for (int i = 0; i < n; ++i) {
         Eff e;
-        rc = make_params(reqs[i].params, e);
-        if (rc) return rc;
-        if (!Launch<T>::xy_supported(e.p.nx) || !Launch<T>::z_supported(e.p.nz))
-            return fail(CB_EUNSUPPORTED, "request %d: grid %d^2x%d not built", i, e.p.nx, e.p.nz);
-        if (pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split) >= 0) continue;
-        const long long bytes = (long long)instance_arena_bytes<T>(e.p);
-        int cap = (int)std::min<long long>(max_slots, budget / std::max<long long>(bytes, 1));
-        cap = std::max(cap, 1);
-        const int tx = Launch<T>::z_tile();
-        rc = pool.add_class(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split, (e.p.ny * e.p.nc + tx - 1) / tx, cap);
-        if (rc) return rc;
+        make_params(reqs[i].params, e);
+        rcls[i] = sv.find(e);
     }
-    rc = pool.build_graph();
-    if (rc) return rc;
-    double* stage = nullptr;
-    long long maxN = 0;
-    for (int i = 0; i < n; ++i)
-        maxN = std::max<long long>(maxN, (long long)reqs[i].params.nx * reqs[i].params.nx * reqs[i].params.nz);
-    CB_CK(cudaMalloc(&stage, (size_t)maxN * sizeof(double)));
-
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
     auto now = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reqs[a].arrival_s < reqs[b].arrival_s; });
+    auto cancel_time = [&](int i) { return reqs[i].cancel_ms > 0 ? reqs[i].arrival_s + 1e-3 * reqs[i].cancel_ms : 0.0; };
     size_t next = 0;
     std::deque<int> queue;
-    std::vector<Active<T>> act;
+    std::vector<Active<T>> act;  // stable indices: finished entries are recycled through `spare`
+    std::vector<int> spare;
     long long used = 0, peak = 0;
     int done = 0, launches = 0;
     double point_steps = 0.0;
-    std::vector<SlotSummary> sum;
+
+    auto finish = [&](int ai, int status_override) -> int {
+        Active<T>& a = act[ai];
+        const int i = a.req;
+        int status = 0;
+        int r = a.st->finish_run(&status);
+        if (r) return r;
+        cb_scalars sc;
+        a.st->scalars(&sc);
+        res[i].finished_s = now();
+        res[i].latency_s = res[i].finished_s - res[i].arrival_s;
+        res[i].E = sc.E;
+        res[i].V = sc.V;
+        res[i].S = sc.S;
+        res[i].steps = sc.steps;
+        res[i].attempts = sc.attempts;
+        res[i].status = status_override >= 0 ? status_override : status;
+        point_steps += (double)a.st->params().N * sc.steps;
+        if (phi_out && phi_out[i]) {
+            r = a.st->get_phi(phi_out[i], false);
+            if (r) return r;
+        }
+        r = sv.retire(a);
+        if (r) return r;
+        used -= a.bytes;
+        a.req = -1;
+        spare.push_back(ai);
+        ++done;
+        return CB_OK;
+    };
+
     while (done < n) {
         const double tnow = now();
         while (next < order.size() && reqs[order[next]].arrival_s <= tnow) queue.push_back(order[next++]);
-        // admission (FIFO, head of line)
-        while (!queue.empty()) {
-            const int i = queue.front();
-            Eff e;
-            make_params(reqs[i].params, e);
-            const long long bytes = (long long)instance_arena_bytes<T>(e.p);
-            const int c = pool.find(e.p.nx, e.p.nz, e.p.method, e.accurate, e.p.split);
-            if (used + bytes > budget || !pool.has_free(c)) break;
-            Active<T> a;
-            a.st.reset(new Stepper<T>());
-            rc = a.st->init(reqs[i].params);
-            if (rc == CB_OK) rc = make_phi0(*a.st, reqs[i], stage);
-            if (rc == CB_OK) rc = a.st->prepare_run(reqs[i].max_steps > 0 ? reqs[i].max_steps : INT_MAX / 2);
-            if (rc == CB_OK) rc = pool.place(a.st.get(), &a.cls, &a.slot);
-            if (rc) { cudaFree(stage); return rc; }
+        // cancellations of queued requests
+        for (auto it = queue.begin(); it != queue.end();) {
+            const double ct = cancel_time(*it);
+            if (ct > 0 && ct <= tnow) {
+                res[*it].arrival_s = reqs[*it].arrival_s;
+                res[*it].finished_s = tnow;
+                res[*it].latency_s = tnow - reqs[*it].arrival_s;
+                res[*it].status = ST_CANCELLED;
+                ++done;
+                it = queue.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        // finished batches: retire what is done or cancelled
+        for (auto& c : sv.cls) {
+            if (!c.inflight || cudaEventQuery(c.ev) == cudaErrorNotReady) continue;
+            CB_CK(cudaEventSynchronize(c.ev));  // reports a failed batch
+            c.inflight = false;
+            for (int k = 0; k < c.cap; ++k) {
+                const int ai = c.slot_act[k];
+                if (ai < 0) continue;
+                const double ct = act[ai].cancel_at;
+                const bool cancelled = ct > 0 && ct <= now();
+                if (!c.h_sum[k].done && !cancelled) continue;
+                rc = finish(ai, c.h_sum[k].done ? -1 : ST_CANCELLED);
+                if (rc) return rc;
+            }
+        }
+        // admission: arrival order; full classes are passed over, the budget stops it
+        for (auto it = queue.begin(); it != queue.end();) {
+            const int i = *it;
+            ServeClass<T>& c = sv.cls[rcls[i]];
+            if (c.inflight || c.active >= c.cap) { ++it; continue; }
+            if (used + c.bytes > budget) break;
+            int ai;
+            if (!spare.empty()) { ai = spare.back(); spare.pop_back(); }
+            else { ai = (int)act.size(); act.emplace_back(); }
+            bool placed = false;
+            rc = sv.admit(reqs[i], rcls[i], act[ai], &placed);
+            if (rc) return rc;
+            if (!placed) { spare.push_back(ai); break; }  // the region is fragmented or full
+            Active<T>& a = act[ai];
             a.req = i;
-            a.bytes = bytes;
-            used += bytes;
+            a.cancel_at = cancel_time(i);
+            c.slot_act[a.slot] = ai;
+            c.active++;
+            used += a.bytes;
             peak = std::max(peak, used);
             res[i].arrival_s = reqs[i].arrival_s;
             res[i].admitted_s = now();
-            res[i].bytes = bytes;
-            queue.pop_front();
-            act.push_back(std::move(a));
+            res[i].bytes = a.bytes;
+            it = queue.erase(it);
         }
-        if (act.empty()) {
+        // every idle class with work starts its next batch
+        bool any = false;
+        for (auto& c : sv.cls) {
+            if (!c.inflight && c.active > 0) {
+                rc = sv.launch(c);
+                if (rc) return rc;
+                launches += c.quantum;
+            }
+            any = any || c.inflight;
+        }
+        if (!any) {
             if (next < order.size()) {
                 const double wait = reqs[order[next]].arrival_s - now();
                 if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
             }
             continue;
         }
-        cudaError_t le = pool.launch(quantum);
-        if (le != cudaSuccess) { cudaFree(stage); return fail(CB_ECUDA, "pool launch: %s", cudaGetErrorString(le)); }
-        launches += quantum;
-        rc = pool.poll(sum);
-        if (rc) { cudaFree(stage); return rc; }
-        for (size_t j = 0; j < act.size();) {
-            const SlotSummary& s = sum[pool.slot_index(act[j].cls, act[j].slot)];
-            if (!s.done) { ++j; continue; }
-            Active<T>& a = act[j];
-            const int i = a.req;
-            int status = 0;
-            a.st->finish_run(&status);
-            cb_scalars sc;
-            a.st->scalars(&sc);
-            res[i].finished_s = now();
-            res[i].latency_s = res[i].finished_s - res[i].arrival_s;
-            res[i].E = sc.E;
-            res[i].V = sc.V;
-            res[i].S = sc.S;
-            res[i].steps = sc.steps;
-            res[i].attempts = sc.attempts;
-            res[i].status = status;
-            point_steps += (double)a.st->params().N * sc.steps;
-            if (phi_out && phi_out[i]) a.st->get_phi(phi_out[i], false);
-            pool.release(a.cls, a.slot);
-            used -= a.bytes;
-            act.erase(act.begin() + j);
-            ++done;
-        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    cudaFree(stage);
     if (stats) {
         stats->wall_s = now();
         stats->completed = done;

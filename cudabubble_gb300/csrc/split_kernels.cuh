@@ -25,6 +25,8 @@ template <class T, int NY, int TX, int NT>
 __global__ void __launch_bounds__(NT) ycol_kernel(const InstT<T>* __restrict__ insts, YArgs a) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
     const InstT<T>& I = insts[blockIdx.y];
     const Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
@@ -144,6 +146,8 @@ __global__ void __launch_bounds__(NT) xrow_kernel(const InstT<T>* __restrict__ i
     constexpr int M = NX / 2, NC = M + 1;
     constexpr int LP = M + 1;  // line pitch in shared memory
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
     const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;

@@ -157,6 +157,12 @@ int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st) {
     return h->impl->shape_adjust(max_steps, st);
 }
 int cb_synchronize(cb_handle* h) { CB_H(h); return h->impl->sync(); }
+int cb_set_launch_limit(cb_handle* h, long long max_graph_launches) {
+    CB_H(h);
+    if (max_graph_launches < 0) return cb::fail(CB_EINVAL, "launch limit < 0");
+    h->impl->set_launch_limit(max_graph_launches);
+    return CB_OK;
+}
 int cb_run_timed(cb_handle* h, int nsteps, long long flush_bytes, double* device_ms, int* attempts) {
     CB_H(h);
     return h->impl->run_timed(nsteps, flush_bytes, device_ms, attempts);

@@ -213,6 +213,12 @@ struct Handle {
     virtual long long bytes() const = 0;
     virtual int run_timed(int nsteps, long long flush_bytes, double* ms, int* attempts) = 0;
     virtual int profile(int nattempts, long long flush_bytes, double* ms, int* cnt) = 0;
+    // bound on the attempt-graph launches of one run / run_timed / shape_adjust call
+    // (0: the built-in no-progress bound, which returns CB_ENOTCONVERGED)
+    void set_launch_limit(long long n) { launch_limit = n > 0 ? n : 0; }
+
+   protected:
+    long long launch_limit = 0;
 };
 
 // kernel kinds reported by cb_profile_kernels
@@ -377,14 +383,19 @@ template <class T> class Stepper final : public Handle {
         if (g_loop) cudaGraphExecDestroy(g_loop);
         if (g_raw) cudaGraphExecDestroy(g_raw);
         if (g_shape) cudaGraphExecDestroy(g_shape);
-        cudaFree(arena);
+        if (!ext_arena) cudaFree(arena);
         cudaFree(scratch);
         cudaFree(cbuf);
         cudaFree(flush_buf);
-        if (st) cudaStreamDestroy(st);
+        if (st && !ext_stream) cudaStreamDestroy(st);
     }
 
-    int init(const cb_params& u) override {
+    int init(const cb_params& u) override { return init_in(u, nullptr, nullptr); }
+
+    // init on caller-owned memory: `mem` (instance_arena_bytes, 256-byte aligned) and
+    // stream `s` are used instead of a cudaMalloc and a new stream, and stay the
+    // caller's (the served pool admits requests into arenas it carved up front)
+    int init_in(const cb_params& u, void* mem, cudaStream_t s) {
         up = u;
         int rc = make_params(u, e);
         if (rc) return rc;
@@ -396,8 +407,17 @@ template <class T> class Stepper final : public Handle {
         ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
         size_t lay[9];
         arena_bytes = instance_arena_bytes<T>(p, lay);
-        CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
+        if (s) {
+            st = s;
+            ext_stream = true;
+        } else {
+            CB_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        }
+        if (mem) {
+            if (reinterpret_cast<uintptr_t>(mem) % 256) return fail(CB_EINVAL, "arena not 256-byte aligned");
+            arena = mem;
+            ext_arena = true;
+        } else if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
             cudaGetLastError();
             return fail(CB_ENOMEM, "cudaMalloc of %zu bytes failed", arena_bytes);
         }
@@ -745,9 +765,15 @@ template <class T> class Stepper final : public Handle {
         CB_CK(cudaEventRecord(e0, st));
         long long launches = 0;
         const long long limit = 70LL * (hc.target + 1LL) + 1000;
+        bool timed_out = false;
         while (!hc.done && launches <= limit) {
-            for (int i = 0; i < 64; ++i) CB_CK(cudaGraphLaunch(g_shape, st));
-            launches += 64;
+            long long chunk = 64;
+            if (launch_limit > 0) {
+                if (launches >= launch_limit) { timed_out = true; break; }
+                chunk = std::min(chunk, launch_limit - launches);
+            }
+            for (long long i = 0; i < chunk; ++i) CB_CK(cudaGraphLaunch(g_shape, st));
+            launches += chunk;
             CB_CK(pull());
         }
         CB_CK(cudaEventRecord(e1, st));
@@ -792,6 +818,8 @@ template <class T> class Stepper final : public Handle {
             out->E_end = fin.E_state;
             out->device_ms = ms;
         }
+        if (timed_out && !fin.done)
+            return fail(CB_ETIMEOUT, "shape adjustment stopped at the launch limit (%lld attempts)", launches);
         if (!fin.done) return fail(CB_ENOTCONVERGED, "shape adjustment made no progress after %lld attempts", launches);
         return CB_OK;
     }
@@ -835,18 +863,19 @@ template <class T> class Stepper final : public Handle {
         CB_CK(cudaEventRecord(e0, st));
         int launches = 0;
         const long long limit = 70LL * (nsteps + 1) * (p.corr ? 2 : 1) + 1000;
+        int stop = CB_OK;  // CB_ETIMEOUT at the caller's launch limit, CB_ENOTCONVERGED at the built-in one
         while (!hc.done) {
             const int remaining = hc.target - hc.steps;
             int chunk = remaining * (p.corr ? 2 : 1) + remaining / 8 + 1;
             chunk = std::max(1, std::min(chunk, 512));
+            if (launch_limit > 0) {
+                if (launches >= launch_limit) { stop = CB_ETIMEOUT; break; }
+                chunk = (int)std::min<long long>(chunk, launch_limit - launches);
+            }
             for (int i = 0; i < chunk; ++i) CB_CK(cudaGraphLaunch(g_loop, st));
             launches += chunk;
             CB_CK(pull());
-            if (launches > limit) {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                return fail(CB_ENOTCONVERGED, "no progress after %d attempts", launches);
-            }
+            if (!hc.done && launches > limit) { stop = CB_ENOTCONVERGED; break; }
         }
         CB_CK(cudaEventRecord(e1, st));
         CB_CK(cudaEventSynchronize(e1));
@@ -866,6 +895,12 @@ template <class T> class Stepper final : public Handle {
         hc.done = 0;
         CB_CK(push());
         CB_CK(cudaStreamSynchronize(st));
+        // a stopped call ends between attempts: the state is the last accepted one and a
+        // further cb_run continues the same trajectory
+        if (stop == CB_ETIMEOUT)
+            return fail(CB_ETIMEOUT, "stopped at the launch limit of %lld attempts (%d of %d steps taken)",
+                        launch_limit, hc.steps - steps0, nsteps);
+        if (stop == CB_ENOTCONVERGED) return fail(CB_ENOTCONVERGED, "no progress after %d attempts", launches);
         switch (last_status) {
             case ST_NONFINITE: return fail(CB_ENONFINITE, "state blew up (non-finite energy)");
             case ST_DT_UNDERFLOW: return fail(CB_EDTUNDERFLOW, "adaptive dt fell below %g", p.dt_min);
@@ -975,7 +1010,9 @@ template <class T> class Stepper final : public Handle {
         double total = 0.0;
         int att = 0;
         const long long limit = 70LL * (nsteps + 1) * (p.corr ? 2 : 1) + 1000;
+        bool timed_out = false;
         while (!hc.done && att < limit) {
+            if (launch_limit > 0 && att >= launch_limit) { timed_out = true; break; }
             if (flush_bytes > 0) CB_CK(cudaMemsetAsync(flush_buf, att & 0xff, (size_t)flush_bytes, st));
             CB_CK(cudaEventRecord(e0, st));
             CB_CK(cudaGraphLaunch(g_loop, st));
@@ -995,6 +1032,7 @@ template <class T> class Stepper final : public Handle {
         CB_CK(cudaStreamSynchronize(st));
         if (ms_out) *ms_out = total;
         if (att_out) *att_out = att;
+        if (timed_out) return fail(CB_ETIMEOUT, "stopped at the launch limit of %lld attempts", launch_limit);
         if (last_status == ST_NONFINITE) return fail(CB_ENONFINITE, "state blew up");
         if (att >= limit) return fail(CB_ENOTCONVERGED, "no progress after %d attempts", att);
         return CB_OK;
@@ -1196,6 +1234,7 @@ template <class T> class Stepper final : public Handle {
     size_t ns = 0;
     int ntiles = 0;
     cudaStream_t st = nullptr;
+    bool ext_arena = false, ext_stream = false;
     InstT<double>* aux = nullptr;  // FP64 descriptor for exact set/get of phi (FP32 form)
     InstT<double> aux_h{};
     cudaGraphExec_t g_loop = nullptr, g_raw = nullptr, g_shape = nullptr;

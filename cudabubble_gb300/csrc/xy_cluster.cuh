@@ -43,6 +43,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     constexpr int M = Q::M, NY = Q::NY, NC = Q::NC, MH = Q::MH, NH = Q::NH, PY = Q::PY, PX = Q::PX;
     constexpr int ntw = sizeof(T) == 4 ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CB_PDL_TRIGGER();
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     const InstT<T>& I = insts[blockIdx.y];
@@ -50,13 +51,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     const Params& p = I.p;
     const int z = blockIdx.x >> 1;
     const int tid = threadIdx.x;
-    // the control fields and this pass's candidate partial sets in one batch of
-    // independent loads (the state-selected pointers are chosen in registers)
-    const int c_done = ctrl->done, c_part = ctrl->part_state, c_u = ctrl->u_state;
     const void *p00 = I.P[0][0], *p01 = I.P[0][1], *p10 = I.P[1][0], *p11 = I.P[1][1], *p20 = I.P[2][0],
                *p21 = I.P[2][1];
     // both CTAs of a cluster hold the same plane of the same instance: they leave together
-    if (z >= p.nz || c_done) return;
+    if (z >= p.nz) return;
     C* S = reinterpret_cast<C*>(smem_raw);
     C* twM = S + Q::SZ;
     C* twN = twM + M;
@@ -75,6 +73,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             for (int i = tid; i < NY; i += NT) twYl[i] = gy[NY + i];
         }
     }
+    // the twiddles (written by no kernel) are loaded; the control state and the
+    // partials come from the previous kernel
+    CB_PDL_WAIT();
+    // the control fields and this pass's candidate partial sets in one batch of
+    // independent loads (the state-selected pointers are chosen in registers)
+    const int c_done = ctrl->done, c_part = ctrl->part_state, c_u = ctrl->u_state;
+    if (c_done) return;
     const PC<T> k(p);
     const size_t plane = (size_t)NY * NC;
     const int set = a.role == R_WORK ? 2 : (a.role == R_STATE ? c_part : 1 - c_part);  // part_set

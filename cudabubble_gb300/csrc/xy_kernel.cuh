@@ -111,20 +111,13 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     constexpr int nf = NF;
     constexpr int pitch = nf * M + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CB_PDL_TRIGGER();
     const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
     const int z = blockIdx.x;
     const int tid = threadIdx.x;
     if (z >= p.nz) return;
-    // the control fields in one batch of independent loads, so the CTA does not wait on a
-    // chain of dependent loads before its data moves
-    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_part = ctrl->part_state, c_u = ctrl->u_state;
-    const bool stepping = a.mode <= XY_FUSED;
-    if (stepping) {
-        if (c_done) return;
-        if (a.skip_if_stale && !c_fresh) return;
-    }
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
     C* twM = S + NY * pitch;                // W_M^m
     C* twN = twM + M;                       // W_NX^m
@@ -145,6 +138,17 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             for (int i = tid; i < M + NX; i += NT) twMl[i] = gx[M + NX + i];
             for (int i = tid; i < NY; i += NT) twYl[i] = gy[NY + i];
         }
+    }
+    // the twiddles (written by no kernel) are loaded; what follows reads the previous
+    // kernel's results
+    CB_PDL_WAIT();
+    // the control fields in one batch of independent loads, so the CTA does not wait on a
+    // chain of dependent loads before its data moves
+    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_part = ctrl->part_state, c_u = ctrl->u_state;
+    const bool stepping = a.mode <= XY_FUSED;
+    if (stepping) {
+        if (c_done) return;
+        if (a.skip_if_stale && !c_fresh) return;
     }
     const T cx = PC<T>(p).cx;
     const size_t plane = (size_t)NY * NC;

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CB_PDL_TRIGGER();
     const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
@@ -142,14 +143,9 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     const int m0 = blockIdx.x * TX;
     const int tid = threadIdx.x;
     if (m0 >= Mc) return;
-    // the control fields and the candidate buffers of this pass in one batch of
-    // independent loads (the state-selected pointer is chosen in registers), so the
-    // CTA does not wait on a chain of dependent loads before its data moves
-    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_ab = ctrl->ab_state;
     const void* g_a[2] = {I.G[0][0], I.G[1][0]};
     const void* g_b[2] = {I.G[0][1], I.G[1][1]};
     const bool plain = a.mode == Z_FWD_PLAIN || a.mode == Z_INV_PLAIN;
-    if (!plain && c_done) return;
     const int ntiles = (Mc + TX - 1) / TX;
     constexpr int W = 2 * TX;  // row pitch: field 0 in [0, TX), field 1 in [TX, 2 TX)
     C* S = reinterpret_cast<C*>(smem_raw);
@@ -158,6 +154,13 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     C* twl = tw + NZ;
     double* red = reinterpret_cast<double*>(tw + ntw * NZ);
     for (int i = tid; i < ntw * NZ; i += NT) tw[i] = reinterpret_cast<const C*>(I.twz)[i];
+    // the twiddles (written by no kernel) are loaded; what follows reads the previous
+    // kernel's results
+    CB_PDL_WAIT();
+    // the control fields in one batch of independent loads (the state-selected pointer
+    // is chosen in registers), so the CTA does not wait on a chain of dependent loads
+    const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_ab = ctrl->ab_state;
+    if (!plain && c_done) return;
 
     const bool stage1 = a.mode == Z_ETD2_S1 || a.mode == Z_ETD4_S1 || a.mode == Z_EULER;
     const bool reuse = stage1 && !c_fresh;  // retry of a rejected step: N_u / R-hat unchanged

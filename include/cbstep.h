@@ -51,7 +51,8 @@ enum { CB_FP64 = 0, CB_FP32 = 1 };
 /* exit reasons reported in cb_scalars.status */
 enum {
     CB_RUNNING = 0, CB_DONE_TARGET = 1, CB_DONE_DT_UNDERFLOW = 2, CB_DONE_SMALL_ENERGY = 3,
-    CB_DONE_NONFINITE = 4, CB_DONE_CONVERGED = 5, CB_DONE_TMAX = 6
+    CB_DONE_NONFINITE = 4, CB_DONE_CONVERGED = 5, CB_DONE_TMAX = 6,
+    CB_DONE_CANCELLED = 7   /* served request cancelled by its client (cb_request.cancel_ms) */
 };
 
 /* field selectors for cb_field (phasefield.cpp getters) */
@@ -190,6 +191,14 @@ int cb_shape_adjust(cb_handle* h, int max_steps, cb_adjust_stats* st);
  * and keeps the fastest for this handle; the state, dt and counters are unchanged */
 int cb_autotune(cb_handle* h, int attempts, cb_tune_result* out);
 int cb_synchronize(cb_handle* h);
+/* no counterpart in the reference, whose loops run until their own exit tests
+ * (belastic.cpp:400-428, :712-740): bounds the attempts (graph launches) that one
+ * cb_run, cb_run_timed or cb_shape_adjust call on this handle may make.  A call that
+ * reaches the bound before its loop ends returns CB_ETIMEOUT; it stops between two
+ * attempts, so the state is the last accepted one and a further call continues the
+ * same trajectory.  0 (the default) keeps only the built-in no-progress bound, which
+ * returns CB_ENOTCONVERGED. */
+int cb_set_launch_limit(cb_handle* h, long long max_graph_launches);
 /* HBM bytes held by the handle's stepping state */
 long long cb_handle_bytes(cb_handle* h);
 
@@ -226,16 +235,24 @@ int cb_batch_run_timed(cb_batch* b, int nsteps, long long flush_bytes, double* d
  * accepted step changes E by less than params.rel_tol |E| (CB_DONE_CONVERGED)
  * or max_steps accepted steps pass (CB_DONE_TARGET: not converged).
  * cb_serve_trace replays an arrival trace in real time with continuous
- * batching: arrivals queue FIFO, the head is admitted while its grid class has
- * a free slot and hbm_budget_bytes holds its state, admitted requests advance
- * together `quantum` attempts at a time and leave as soon as they finish. */
+ * batching.  Requests of one (grid, method) form a size class with its own
+ * slot table, attempt graph and stream, so classes advance independently and
+ * their work overlaps on the device.  Arrivals queue in arrival order; each
+ * pass admits every queued request whose class has a free slot (a full class
+ * is passed over) while hbm_budget_bytes holds its state (a request the
+ * budget cannot hold stops admission behind it).  Instances live in arenas
+ * carved from one device region reserved before the trace starts, so
+ * admission allocates nothing.  A class runs `quantum` attempts per batch
+ * (more for grids below 128^3, whose attempts are short), retires the
+ * requests that finished or were cancelled, admits new ones and starts its
+ * next batch at once. */
 typedef struct cb_request {
     cb_params params;
     double axes[3], centre[3];    /* ellipsoid semi-axes and centre */
     double axes2[3], centre2[3];  /* optional second ellipsoid (union) when axes2[0] > 0 */
     double arrival_s;             /* arrival time from the start of the trace */
     int max_steps;
-    int pad;
+    int cancel_ms;                /* > 0: the client cancels the request this many ms after its arrival */
 } cb_request;
 
 typedef struct cb_result {
@@ -257,18 +274,21 @@ typedef struct cb_serve_stats {
 int cb_serve_trace(const cb_request* reqs, int n, long long hbm_budget_bytes, int max_slots_per_class, int quantum,
                    cb_result* results, double** phi_out, cb_serve_stats* stats);
 
-/* (mean(u) + addition) * multiply * volume of a device-resident real field
- * d_u[nz][ny][nx], written to the device double *d_val on `stream` (a
- * cudaStream_t; NULL is the legacy default stream).  Same quantity as the
- * reference's Calc::intf (Calc.cu:191-262), but no counterpart there: this
- * entry point allocates nothing.  Its partial sums live in a fixed file-scope
- * device array of 4096 planes (32 KiB), so nz > 4096 returns CB_EINVAL; it is
- * meant for callers that may not allocate device memory at the point of the
- * call (a carved-up memory pool, a host that forbids allocations after
- * start-up).  The first call on each device does a synchronous set-up
- * (resolves the array's address, clears its counter): make it before any
- * stream capture.  All calls on a device share the one array, so calls that
- * overlap in time (other streams, other host threads) race; serialise them. */
+/* No counterpart in the reference: an allocation-free volume integral.
+ * Computes (mean(u) + addition) * multiply * volume of a device-resident real
+ * field d_u[nz][ny][nx] and writes it to the device double *d_val on `stream`
+ * (a cudaStream_t; NULL is the legacy default stream).  With addition 1 and
+ * multiply 1/2 it is the vesicle volume; with addition 0 it integrates a
+ * density (the surface term, f^2).  It allocates nothing: its per-plane
+ * partial sums live in a fixed file-scope device array of 4096 planes
+ * (32 KiB), so nz > 4096 returns CB_EINVAL.  It is meant for callers that may
+ * not allocate device memory at the point of the call (a carved-up memory
+ * pool, a host that forbids allocations after start-up).  The first call on
+ * each device (and after a context rebuild) clears the array's counter
+ * synchronously: make it before any stream capture.  All calls on a device
+ * share the one array and each call leaves it ready for the next, so calls
+ * that overlap in time (other streams, other host threads) race; serialise
+ * them. */
 int cb_intf_noalloc(const double* d_u, int nx, int ny, int nz, double addition, double multiply, double volume,
                     double* d_val, void* stream);
 

@@ -2,8 +2,8 @@
 # Builds the reference's own FP64 cuFFT stepper plus the step-by-step harness
 # (harness.cpp) into oracle/_ref/refstep.  TEST INFRASTRUCTURE ONLY.
 #
-# Sources: the reference tree given by $CB_REFERENCE_SRC (default
-# /root/reference).  When that tree exists, the needed files are staged,
+# Sources: the reference tree given by $CB_REFERENCE_SRC (default: a directory
+# named "reference" beside the repository).  When that tree exists, the needed files are staged,
 # unmodified, into oracle/_ref/src/ (git-ignored) so that a machine without
 # the reference tree (the GPU host) can rebuild from the staged copy.  No
 # reference file is edited: CUDA-13 API drift is absorbed by the forced-include
@@ -13,7 +13,7 @@ here="$(cd "$(dirname "$0")" && pwd)"
 root="$(cd "$here/../.." && pwd)"
 out="$root/oracle/_ref"
 src="$out/src"
-ref="${CB_REFERENCE_SRC:-/root/reference}"
+ref="${CB_REFERENCE_SRC:-$root/../reference}"
 files="Calc.cu Calc.h belastic.cpp belastic.h fluidbase.cpp fluidbase.h phasefield.cpp phasefield.h
        tool.cpp tool.cu tool.h mem_array.cpp mem_array.h stdafx.h drawbubble.cpp stb_image.h
        stb_image_write.h stb_image_resize.h"

@@ -30,11 +30,14 @@ def test_autotune_keeps_the_state_and_picks_a_timed_path(cblib, n, prec):
     assert r["path"] in r["timed"] and all(v > 0 for v in r["timed"].values())
     if prec == 1:
         assert capi.XYP_CLUSTER in r["timed"] and capi.XYP_SINGLE in r["timed"]
-    # the tuned handle continues exactly as one created on the chosen path
+    st.close()
+    # a handle tuned before its first step runs exactly as one created on the chosen path
+    # (the paths sum in different orders, so the comparison starts from the same phi0)
+    st = _stepper(capi, n, n, prec, capi.XYP_AUTO)
+    r = st.autotune(8)
     other = _stepper(capi, n, n, prec, r["path"])
-    other.run(5)
-    st.run(20)
-    other.run(20)
+    st.run(25)
+    other.run(25)
     assert np.array_equal(st.get_phi(), other.get_phi())
     st.close()
     other.close()

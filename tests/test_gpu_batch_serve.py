@@ -83,3 +83,47 @@ def test_server_results_same_alone_and_in_mix(cblib):
                                         phi_out={0: want[i]})
         assert (alone[0]["steps"], alone[0]["E"]) == (r["steps"], r["E"]), i
         assert np.array_equal(ph[0], phis[i]), i
+
+
+def test_server_cancellation_frees_the_slot_and_budget(cblib):
+    """A client cancels one running request and one queued request.  The budget holds
+    one 32^3 instance at a time, so the requests behind the running one wait for its
+    memory: it is retired with CB_DONE_CANCELLED after its class's current batch, its
+    bytes go back, and the next request is admitted and finishes as it would alone."""
+    from cudabubble_gb300 import capi
+    r0 = _request(capi, 32, 200, 0.000)
+    r1 = _request(capi, 32, 201, 0.001, rel_tol=0.0, max_steps=10 ** 7)  # runs until cancelled
+    r1.cancel_ms = 200
+    r2 = _request(capi, 32, 202, 0.002)
+    r3 = _request(capi, 32, 203, 0.003)  # cancelled while it waits in the queue
+    r3.cancel_ms = 50
+    reqs = [r0, r1, r2, r3]
+    budget = int(1.5 * cblib.cb_instance_bytes(r0.params))
+    res, stats, _ = capi.serve_trace(reqs, budget, max_slots_per_class=4, quantum=2)
+    assert stats["completed"] == 4
+    assert stats["peak_bytes"] <= budget
+    assert res[0]["status"] in (capi.CB_DONE_TARGET, capi.CB_DONE_CONVERGED)
+    assert res[1]["status"] == capi.CB_DONE_CANCELLED
+    assert res[1]["admitted_s"] > 0 and res[1]["steps"] > 0
+    assert res[1]["finished_s"] >= 0.201 - 1e-3
+    assert res[3]["status"] == capi.CB_DONE_CANCELLED
+    assert res[3]["admitted_s"] == 0.0 and res[3]["steps"] == 0
+    assert 0.053 - 1e-3 <= res[3]["finished_s"] < res[1]["finished_s"]
+    # the request behind the cancelled one got its memory and ran to its own end
+    assert res[2]["admitted_s"] >= res[1]["finished_s"] - 1e-3
+    assert res[2]["status"] in (capi.CB_DONE_TARGET, capi.CB_DONE_CONVERGED)
+    alone, _, _ = capi.serve_trace([r2], budget, max_slots_per_class=4, quantum=2)
+    assert (alone[0]["steps"], alone[0]["E"]) == (res[2]["steps"], res[2]["E"])
+
+
+def test_server_passes_over_a_full_class(cblib):
+    """A full class does not hold up requests of other classes behind it."""
+    from cudabubble_gb300 import capi
+    big = [_request(capi, 48, 300 + i, 0.0, rel_tol=0.0, max_steps=400) for i in range(2)]
+    small = _request(capi, 16, 310, 0.001, max_steps=50)
+    res, stats, _ = capi.serve_trace(big + [small], 10 ** 10, max_slots_per_class=1, quantum=2)
+    assert stats["completed"] == 3
+    # the second 48^3 request waits for the first one's slot; the 16^3 one does not
+    assert res[1]["admitted_s"] >= res[0]["finished_s"] - 1e-3
+    assert res[2]["admitted_s"] < res[0]["finished_s"]
+    assert res[2]["finished_s"] < res[1]["finished_s"]

@@ -15,6 +15,8 @@ import subprocess
 
 import pytest
 
+pytestmark = pytest.mark.emulation
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "cudabubble_gb300", "csrc")
 EMU = os.path.join(ROOT, "tests", "emu")
