@@ -106,7 +106,16 @@ static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& 
     return cudaErrorInvalidValue;
 }
 
-template <class T> constexpr int ztile() { return sizeof(T) == 4 ? 16 : 8; }
+// z-pass tile of the FP32 form: columns per CTA and threads per CTA (build-time knobs;
+// the FP64 form keeps 8 columns of 16-byte values and 256 threads)
+#ifndef CB_Z_TX
+#define CB_Z_TX 16
+#endif
+#ifndef CB_Z_NT
+#define CB_Z_NT 256
+#endif
+template <class T> constexpr int ztile() { return sizeof(T) == 4 ? CB_Z_TX : 8; }
+template <class T> constexpr int zthreads() { return sizeof(T) == 4 ? CB_Z_NT : 256; }
 
 // ---- split plane path
 template <int NX> constexpr int split_rpc() { return NX >= 96 ? 16 : 8; }
@@ -114,7 +123,7 @@ constexpr int kSplitThreads = 256;
 
 template <class T, int NY>
 static cudaError_t ycol_go(const InstT<T>* d, int ninst, int nzmax, const YArgs& a, cudaStream_t s) {
-    constexpr int TX = ztile<T>(), NT = kSplitThreads;
+    constexpr int TX = sizeof(T) == 4 ? 16 : 8, NT = kSplitThreads;  // the split path's own column tile
     constexpr size_t sm = ycol_smem_bytes<T, NY, TX>();
     static bool attr = false;
     if (!attr) {
@@ -185,7 +194,7 @@ static cudaError_t xy_split_go(const InstT<T>* d, int ninst, int nzmax, const XY
 template <class T, int NZ, int MG>
 static cudaError_t z_go_g(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
     constexpr int TX = ztile<T>();
-    constexpr int NT = 256;
+    constexpr int NT = zthreads<T>();
     constexpr size_t sm = z_smem_bytes<T, NZ, TX>();
     static bool attr = false;
     if (!attr) {

@@ -114,10 +114,11 @@ template <> struct State<float> {
     }
 };
 
-// resident CTAs per SM the z pass is compiled for (its register cap); the pass waits
-// on global loads, so more resident warps hide more of them
-#ifndef CB_Z_MINB
-#define CB_Z_MINB 4
+// resident threads per SM the z pass is compiled for (its register cap: 64 registers a
+// thread at 1024); the pass is latency-bound, and fewer resident warps cost more than
+// the registers buy (768 threads: 28 % slower at 128^3)
+#ifndef CB_Z_THREADS_PER_SM
+#define CB_Z_THREADS_PER_SM 1024
 #endif
 
 // Mode groups: each z_kernel instance compiles only its group's stage code, so
@@ -130,7 +131,7 @@ __host__ __device__ constexpr int zgroup_of(int mode) {
 }
 
 template <class T, int NZ, int TX, int NT, int MG>
-__global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+__global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -165,6 +166,31 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     const bool stage1 = a.mode == Z_ETD2_S1 || a.mode == Z_ETD4_S1 || a.mode == Z_EULER;
     const bool reuse = stage1 && !c_fresh;  // retry of a rejected step: N_u / R-hat unchanged
     const bool need_fwd = (a.mode <= Z_EULER && !reuse) || a.mode == Z_FWD_PLAIN;
+    // thread 0 forms the CTA's scalars from the control state now, so its chain of global
+    // loads and FP64 arithmetic runs under the forward loads and transform rather than
+    // while the block waits (a barrier before the combine publishes them)
+    T* bc = reinterpret_cast<T*>(red);  // dt * ga and (FP32 form) the lambda terms, once per CTA
+    if (tid == 0) {
+        bc[0] = (T)(ctrl->dt * p.ga);
+        if constexpr (sizeof(T) == 4) {  // of the state the fused pass evaluated
+            if (a.mode <= Z_EULER) {
+                const int role = stage1 ? R_STATE : R_WORK;
+                nonlin_lambdas<T>(p, ctrl, role, bc + 1);
+                // N'(k = 0) whole, in FP64, from the fused pass's FP64 totals of G'' and
+                // w (or f): its terms (mean G'', the lambda1 constant, lambda2 f-hat(0))
+                // are ~1e2..1e3 and cancel to O(1), so summed in FP32 they move the
+                // volume by ~1e-4 of its step-to-step change, and E with it through the
+                // M1 penalty
+                const Scal& sc = ctrl->sc[role];
+                const bool euler = p.method == M_EULER;
+                const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
+                const double h0 = sc.sum_h * p.invN;
+                const double n0 = euler ? sc.sum_g * p.invN + 0.5 * lam1 + lam2 * h0
+                                        : sc.sum_g * p.invN - 0.5 * lam1 - 1.0606601717798212866 * lam2 * h0 * p.d_ieps;
+                bc[3] = (T)n0;
+            }
+        }
+    }
 
     if (need_fwd) {
         // stage 1 of the FP32 form reads the state's fused-pass outputs (G slot)
@@ -239,28 +265,6 @@ __global__ void __launch_bounds__(NT, CB_Z_MINB) z_kernel(const InstT<T>* __rest
     C* Nb = reinterpret_cast<C*>(I.Nb);
     void* ah = I.ahat;
     const T* coef = I.coef + (size_t)ctrl->tab_cur * (size_t)(p.kmax + 1) * 8;
-    T* bc = reinterpret_cast<T*>(red);  // dt * ga and (FP32 form) the lambda terms, once per CTA
-    if (tid == 0) {
-        bc[0] = (T)(ctrl->dt * p.ga);
-        if constexpr (sizeof(T) == 4) {  // of the state the fused pass evaluated
-            if (a.mode <= Z_EULER) {
-                const int role = stage1 ? R_STATE : R_WORK;
-                nonlin_lambdas<T>(p, ctrl, role, bc + 1);
-                // N'(k = 0) whole, in FP64, from the fused pass's FP64 totals of G'' and
-                // w (or f): its terms (mean G'', the lambda1 constant, lambda2 f-hat(0))
-                // are ~1e2..1e3 and cancel to O(1), so summed in FP32 they move the
-                // volume by ~1e-4 of its step-to-step change, and E with it through the
-                // M1 penalty
-                const Scal& sc = ctrl->sc[role];
-                const bool euler = p.method == M_EULER;
-                const double lam1 = p.M1 * (sc.V - ctrl->alpha), lam2 = p.M2 * (sc.S - ctrl->beta);
-                const double h0 = sc.sum_h * p.invN;
-                const double n0 = euler ? sc.sum_g * p.invN + 0.5 * lam1 + lam2 * h0
-                                        : sc.sum_g * p.invN - 0.5 * lam1 - 1.0606601717798212866 * lam2 * h0 * p.d_ieps;
-                bc[3] = (T)n0;
-            }
-        }
-    }
     __syncthreads();
     const T dtga = bc[0];
     const T g_f = sizeof(T) == 4 ? bc[2] : (T)0;  // bc[1], the lambda1 constant, enters n0
