@@ -34,14 +34,21 @@ def nvcc() -> str:
 STAMP = os.path.join(LIBDIR, "build_defines.txt")
 
 
+SCHEDULE = os.path.join(PKG, "schedule.txt")
+
+
 def defines() -> list[str]:
-    """Extra -D flags from CB_NVCC_DEFINES (launch-shape tuning, e.g.
-    -DCB_XY_NT_LARGE=1024); the library is rebuilt whenever they change."""
-    return [d for d in os.environ.get("CB_NVCC_DEFINES", "").split() if d.startswith("-D")]
+    """Extra -D flags for the launch schedules (z tile, thread counts, plane FFT split):
+    CB_NVCC_DEFINES when set, else the schedule the tuner (tune.py) chose, kept in
+    schedule.txt; the library is rebuilt whenever they change."""
+    env = os.environ.get("CB_NVCC_DEFINES")
+    if env is None and os.path.exists(SCHEDULE):
+        env = " ".join(l.split("#")[0] for l in open(SCHEDULE))
+    return [d for d in (env or "").split() if d.startswith("-D")]
 
 
-def _compile(src: str) -> str:
-    obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+def _compile(src: str, build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, os.path.splitext(os.path.basename(src))[0] + ".o")
     cmd = [nvcc(), "-std=c++17", *ARCH, "-lineinfo", "-O3", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
            *defines(), "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
@@ -59,26 +66,34 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB)
     for d in (CSRC, INCLUDE, PKG):
         for f in os.listdir(d):
-            if not os.path.isfile(os.path.join(d, f)) or not f.endswith((".cu", ".cuh", ".h", "build.py")):
+            if not os.path.isfile(os.path.join(d, f)) or not f.endswith((".cu", ".cuh", ".h", "build.py",
+                                                                            "schedule.txt")):
                 continue
             if os.path.getmtime(os.path.join(d, f)) > t:
                 return True
     return False
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+def build_to(lib: str, build_dir: str) -> str:
+    """Compile every translation unit with the current defines into `build_dir` and link
+    the shared library at `lib`."""
+    os.makedirs(build_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, build_dir), SOURCES))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
+    return lib
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and not _stale():
+        return LIB
+    build_to(LIB, BUILD)
     with open(STAMP, "w") as f:
         f.write(" ".join(defines()))
     if verbose:

@@ -12,7 +12,9 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "lib", "libcbstep.so")
+# CB_LIB names another build of the library (the schedule tuner times candidate builds
+# in child processes this way)
+LIB_PATH = os.environ.get("CB_LIB") or os.path.join(_HERE, "lib", "libcbstep.so")
 
 CB_OK, CB_EINVAL, CB_ENOMEM, CB_ECUDA, CB_ENONFINITE, CB_ENOTCONVERGED, CB_ETIMEOUT, CB_EDTUNDERFLOW, \
     CB_EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8

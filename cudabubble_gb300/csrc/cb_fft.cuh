@@ -244,8 +244,18 @@ template <> struct Plan<24> { static constexpr int R1 = 8, R2 = 3; };
 template <> struct Plan<32> { static constexpr int R1 = 8, R2 = 4; };
 template <> struct Plan<48> { static constexpr int R1 = 8, R2 = 6; };
 template <> struct Plan<64> { static constexpr int R1 = 8, R2 = 8; };
+// the split of the 96- and 128-point lines is a build-time schedule (CB_PLAN96_12X8,
+// CB_PLAN128_8X16), chosen with the launch shapes by the schedule tuner (tune.py)
+#ifdef CB_PLAN96_12X8
+template <> struct Plan<96> { static constexpr int R1 = 12, R2 = 8; };
+#else
 template <> struct Plan<96> { static constexpr int R1 = 16, R2 = 6; };
+#endif
+#ifdef CB_PLAN128_8X16
+template <> struct Plan<128> { static constexpr int R1 = 8, R2 = 16; };
+#else
 template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
+#endif
 template <> struct Plan<192> { static constexpr int R1 = 16, R2 = 12; };
 template <> struct Plan<256> { static constexpr int R1 = 16, R2 = 16; };
 
