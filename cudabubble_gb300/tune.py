@@ -11,7 +11,9 @@ build of the library, timed in a process of its own:
 A coordinate search starts from the default schedule and, knob by knob, keeps the
 candidate with the lowest weighted device time per attempt of the FP32 ETD-RK2 loop on
 the given grid sizes (seeded ellipsoids, the L2 flushed between attempts).  Candidates
-whose energies leave the default's by more than 1e-5 are refused.  With --write the
+whose energies leave the default's by more than 1e-5 are refused, and a knob moves off
+its current option only for a gain of at least --min-gain (1 %: run-to-run spread, and
+a line split changes the FP32 rounding).  With --write the
 winner goes to cudabubble_gb300/schedule.txt, which build.py compiles with from then
 on (CB_NVCC_DEFINES overrides it).
 
@@ -77,7 +79,7 @@ def _measure(defs, sizes, steps):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-def tune(sizes, weights, steps, write=False, log=print):
+def tune(sizes, weights, steps, write=False, log=print, min_gain=0.01):
     choice = [opts[0] for _, opts in KNOBS]
     flat = lambda ch: [d for opt in ch for d in opt]
     cache = {}
@@ -104,7 +106,7 @@ def tune(sizes, weights, steps, write=False, log=print):
             drift = max(abs(res[str(n)]["E"] - ref[str(n)]["E"]) / abs(ref[str(n)]["E"]) for n in sizes)
             table.append((" ".join(flat(trial)) or "(defaults)", c))
             log(f"  {name}: {' '.join(opt) or 'default'} -> {c:.4f} ms (energy drift {drift:.1e})")
-            if drift <= 1e-5 and c < best_cost:
+            if drift <= 1e-5 and c < best_cost and c < cost(choice)[0] * (1.0 - min_gain):
                 best, best_cost = opt, c
         choice[i] = best
         log(f"{name}: keep {' '.join(best) or 'default'}")
@@ -127,6 +129,7 @@ def main():
     ap.add_argument("--weights", default="")
     ap.add_argument("--steps", type=int, default=120)
     ap.add_argument("--write", action="store_true")
+    ap.add_argument("--min-gain", type=float, default=0.01)
     ap.add_argument("--child", action="store_true")
     a = ap.parse_args()
     sizes = [int(x) for x in a.sizes.split(",")]
@@ -134,7 +137,7 @@ def main():
         _child(sizes, a.steps)
         return
     weights = [float(x) for x in a.weights.split(",")] if a.weights else [1.0] * len(sizes)
-    final, table = tune(sizes, weights, a.steps, a.write)
+    final, table = tune(sizes, weights, a.steps, a.write, min_gain=a.min_gain)
     print(json.dumps({"schedule": final, "timed": [{"defines": k, "ms": c} for k, c in table]}))
 
 
