@@ -285,6 +285,15 @@ struct PairRows {
     }
 };
 
+// three fields: rows of field 0 and field 1 side by side in one padded plane (as
+// PairRows), then rows of a third field in a region of its own, QOFF slots in, pitch QX
+template <int N1, int PITCH, int SECOND, int QOFF, int QX>
+struct TripleRows {
+    __device__ __forceinline__ int operator()(int l) const {
+        return (l < N1) ? l * PITCH : (l < 2 * N1) ? (l - N1) * PITCH + SECOND : QOFF + (l - 2 * N1) * QX;
+    }
+};
+
 // NT: natural in -> transposed out.  Lines l in [0, nlines) at buf + off(l),
 // element stride es.  All NTHR threads of the block call it; caller syncs after.
 template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>

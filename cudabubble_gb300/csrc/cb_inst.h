@@ -85,6 +85,8 @@ struct Params {
     int grow_every;     // grow dt every this many accepted steps
     int split;          // 1: split plane passes for every xy mode
     int sched;          // SCHED_LOOP: the time loops; SCHED_SHAPE: the shape_adjust rules
+    int curv;           // FP32 form with C != 0: the fused passes carry a third field q (InstT::Q, G[.][2])
+    int pad_curv;
     double eps, eta, ga, M1, M2;
     double cx;          // (2 pi / L)^2
     double L3;          // box volume
@@ -93,7 +95,7 @@ struct Params {
     double tmax;        // Euler loop time limit (belastic.cpp:407)
     double rel_tol;     // > 0: stop once an accepted step changes E by < rel_tol |E|
     double reject_tol;  // adaptive: reject when E_new > E_old + reject_tol |E_old|
-    double C;           // spontaneous curvature (plain FP64 form; 0 in the reference)
+    double C;           // spontaneous curvature (0 in the reference)
     // host-precomputed constants: GB300 runs FP64 at a small fraction of its
     // FP32 rate, so kernels read these instead of dividing per thread
     double d_ieps, d_ieps2, d_ieps3, d_bnl;  // 1/eps, 1/eps^2, 1/eps^3, beta * cx
@@ -101,17 +103,20 @@ struct Params {
     // the same constants split hi + lo for the FP32 form's compensated
     // products (KC<float>): eps, 1/eps, eta/eps^2, eta D/eps^3, beta cx, 1/N, cx
     float fk[7][2];
+    // FP32 form with curvature: C, the third field's factor (eps C for ETD, C for Euler)
+    // and 2 eps C
+    float f_C, f_qC, f_2eC, f_padc;
 };
 enum { FK_EPS = 0, FK_IEPS, FK_K2, FK_K3, FK_BNL, FK_INVN, FK_CX };
 
 // the precomputed constants in the kernel's precision
 template <class T> struct PC;
 template <> struct PC<float> {
-    float eps, ieps, ieps2, ieps3, bnl, cx, invN, eta;
+    float eps, ieps, ieps2, ieps3, bnl, cx, invN, eta, C, qC, e2C;
     KC<float> k_eps, k_ieps, k_K2, k_K3, k_bnl, k_invN, k_cx;
     __device__ __forceinline__ explicit PC(const Params& p)
         : eps(p.f_eps), ieps(p.f_ieps), ieps2(p.f_ieps2), ieps3(p.f_ieps3), bnl(p.f_bnl), cx(p.f_cx),
-          invN(p.f_invN), eta(p.f_eta), k_eps{p.fk[FK_EPS][0], p.fk[FK_EPS][1]},
+          invN(p.f_invN), eta(p.f_eta), C(p.f_C), qC(p.f_qC), e2C(p.f_2eC), k_eps{p.fk[FK_EPS][0], p.fk[FK_EPS][1]},
           k_ieps{p.fk[FK_IEPS][0], p.fk[FK_IEPS][1]}, k_K2{p.fk[FK_K2][0], p.fk[FK_K2][1]},
           k_K3{p.fk[FK_K3][0], p.fk[FK_K3][1]}, k_bnl{p.fk[FK_BNL][0], p.fk[FK_BNL][1]},
           k_invN{p.fk[FK_INVN][0], p.fk[FK_INVN][1]}, k_cx{p.fk[FK_CX][0], p.fk[FK_CX][1]} {}
@@ -142,7 +147,9 @@ template <class T> struct InstT {
     void* A;
     void* B;
     void* Y[2];       // split plane path: y-transformed fields (nullptr when unused)
-    void* G[2][2];    // FP32 form: XY_FUSED outputs (G'', w) of the state / candidate (ctrl->ab_state)
+    void* G[2][3];    // FP32 form: XY_FUSED outputs (G'', w, and q with curvature) of the state /
+                      // candidate (ctrl->ab_state)
+    void* Q;          // FP32 form with curvature: the work stage's third partial (q)
     // FP32 form: real-space u of the state / candidate as double-float pairs, rows
     // [z][y] of nx/2 float4 (two points each) in the fused passes' x-slot order
     // (ctrl->u_state).  The z pass transforms only u - u_state, and the

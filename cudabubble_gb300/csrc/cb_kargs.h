@@ -16,7 +16,7 @@ struct XYArgs {
     int mode;
     int role;           // partial set and Scal record the pass reads / writes
     int skip_if_stale;  // XY_NONLIN on the state: skip when the stored N_u is reused
-    int pad;
+    int curv;           // FP32 XY_FUSED with spontaneous curvature: the third output field q
     const void* cin;    // XY_INV_PLAIN: partial C[nz][ny][nc]
     double* rout;       // XY_INV_PLAIN: real double[nz][ny][nx]
     const double* rin;  // XY_FWD_PLAIN: real double[nz][ny][nx]
@@ -61,6 +61,8 @@ struct ZArgs {
     int role;      // partial set / Scal record written (stage modes), spectrum read (Z_INV_STATE)
     int mul;       // SpecMul for Z_INV_PLAIN
     int state_io;  // IO_* bits (Z_FWD_PLAIN / Z_INV_PLAIN)
+    int curv;      // FP32 stage modes with spontaneous curvature: the third partial q
+    int pad;
     const void* cin;
     void* cout;
 };

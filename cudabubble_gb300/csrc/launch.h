@@ -12,9 +12,10 @@ template <class T> struct Launch {
     static bool xy_supported(int nx);        // stepping (single-CTA planes or the split path)
     static bool z_supported(int nz);
     static bool xy_plain_supported(int nx);  // plain transforms
-    static bool xy_single(int nx, int nf);   // one CTA per plane holds nf fields
+    static bool xy_single(int nx, int nf, int curv = 0);  // one CTA per plane holds nf fields (+ q)
     static bool xy_split_supported(int nx);
-    static bool xy_cluster_ok(int nx);       // FP32 fused pass on two-CTA clusters
+    static bool xy_cluster_ok(int nx, int curv = 0);      // FP32 fused pass on two-CTA clusters (+ q)
+    static bool fused_curv_ok(int nx, int path);          // FP32 fused pass with curvature on `path`
     static int xy_rows_per_cta(int nx);      // split path: rows of the x pass per CTA
     static int z_tile();
     // path: an XYPath.  XYP_SINGLE falls back to the split passes where one plane does not

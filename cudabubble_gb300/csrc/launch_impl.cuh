@@ -54,45 +54,57 @@ template <class T, int NX> struct XYCfg {
     static constexpr int NT_NONLIN = NX <= 64 ? NT : CB_XY_NT_NONLIN;
     static constexpr bool ok = xy_smem_bytes<T, NX>(2) <= kMaxSmem;   // stepping (two fields)
     static constexpr bool ok1 = xy_smem_bytes<T, NX>(1) <= kMaxSmem;  // plain transforms (one field)
+    // the FP32 fused pass with curvature (a third output field)
+    static constexpr bool ok_q = sizeof(T) == 4 && xy_smem_bytes<T, NX>(2, 1) <= kMaxSmem;
 };
 
 // FP32 fused pass on two-CTA clusters from 64^2 planes (a build-time knob)
 #ifndef CB_XY_CLUSTER
 #define CB_XY_CLUSTER 1
 #endif
-template <class T, int NX> constexpr bool xyc_ok() {
-    return CB_XY_CLUSTER && sizeof(T) == 4 && NX >= 64 && NX % 4 == 0 && xyc_smem_bytes<T, NX>() <= 227 * 1024;
+template <class T, int NX, int NQ = 0> constexpr bool xyc_ok() {
+    return CB_XY_CLUSTER && sizeof(T) == 4 && NX >= 64 && NX % 4 == 0 && xyc_smem_bytes<T, NX, NQ>() <= 227 * 1024;
 }
-template <class T, int NX>
+template <class T, int NX, int NQ = 0>
 static cudaError_t xyc_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
     constexpr int NT = NX >= 96 ? 512 : 256;
-    constexpr size_t sm = xyc_smem_bytes<T, NX>();
+    constexpr size_t sm = xyc_smem_bytes<T, NX, NQ>();
     static bool attr = false;
     if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(xyc_fused_kernel<T, NX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t e = cudaFuncSetAttribute(xyc_fused_kernel<T, NX, NT, NQ>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    return launch_k(xyc_fused_kernel<T, NX, NT>, dim3(2 * nzmax, ninst), dim3(NT), sm, s, d, a);
+    return launch_k(xyc_fused_kernel<T, NX, NT, NQ>, dim3(2 * nzmax, ninst), dim3(NT), sm, s, d, a);
 }
 
-template <class T, int NX, int NF, int NT>
+template <class T, int NX, int NF, int NT, int NQ = 0>
 static cudaError_t xy_go_nf(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s) {
+    constexpr size_t sm = xy_smem_bytes<T, NX>(NF, NQ);
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)xy_smem_bytes<T, NX>(NF));
+        cudaError_t e = cudaFuncSetAttribute(xy_kernel<T, NX, NT, NF, NQ>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    return launch_k(xy_kernel<T, NX, NT, NF>, dim3(nzmax, ninst), dim3(NT), xy_smem_bytes<T, NX>(NF), s, d, a);
+    return launch_k(xy_kernel<T, NX, NT, NF, NQ>, dim3(nzmax, ninst), dim3(NT), sm, s, d, a);
 }
 
 template <class T, int NX>
 static cudaError_t xy_go(const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
                          bool allow_cluster) {
     const bool two = a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED;
+    if constexpr (sizeof(T) == 4) {
+        if (a.curv && a.mode == XY_FUSED) {  // the fused pass with its third field q
+            if constexpr (xyc_ok<T, NX, 1>()) {
+                if (allow_cluster) return xyc_go<T, NX, 1>(d, ninst, nzmax, a, s);
+            }
+            if constexpr (XYCfg<T, NX>::ok_q) return xy_go_nf<T, NX, 2, XYCfg<T, NX>::NT_NONLIN, 1>(d, ninst, nzmax, a, s);
+            return cudaErrorInvalidValue;
+        }
+    }
     if constexpr (xyc_ok<T, NX>()) {
         if (a.mode == XY_FUSED && allow_cluster) return xyc_go<T, NX>(d, ninst, nzmax, a, s);
     }
@@ -191,23 +203,33 @@ static cudaError_t xy_split_go(const InstT<T>* d, int ninst, int nzmax, const XY
     return r;
 }
 
-template <class T, int NZ, int MG>
+template <class T, int NZ, int MG, int NQ = 0>
 static cudaError_t z_go_g(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
     constexpr int TX = ztile<T>();
     constexpr int NT = zthreads<T>();
-    constexpr size_t sm = z_smem_bytes<T, NZ, TX>();
+    constexpr size_t sm = z_smem_bytes<T, NZ, TX, NQ>();
     static bool attr = false;
     if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(z_kernel<T, NZ, TX, NT, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t e = cudaFuncSetAttribute(z_kernel<T, NZ, TX, NT, MG, NQ>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    return launch_k(z_kernel<T, NZ, TX, NT, MG>, dim3(ntiles, ninst), dim3(NT), sm, s, d, a);
+    return launch_k(z_kernel<T, NZ, TX, NT, MG, NQ>, dim3(ntiles, ninst), dim3(NT), sm, s, d, a);
 }
 
 template <class T, int NZ>
 static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a, cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        if (a.curv) {  // FP32 stages with spontaneous curvature: the third partial q
+            switch (zgroup_of(a.mode)) {
+                case ZG_ETD2: return z_go_g<T, NZ, ZG_ETD2, 1>(d, ninst, ntiles, a, s);
+                case ZG_ETD4: return z_go_g<T, NZ, ZG_ETD4, 1>(d, ninst, ntiles, a, s);
+                case ZG_EULER: return z_go_g<T, NZ, ZG_EULER, 1>(d, ninst, ntiles, a, s);
+                default: break;
+            }
+        }
+    }
     switch (zgroup_of(a.mode)) {
         case ZG_ETD2: return z_go_g<T, NZ, ZG_ETD2>(d, ninst, ntiles, a, s);
         case ZG_ETD4: return z_go_g<T, NZ, ZG_ETD4>(d, ninst, ntiles, a, s);
@@ -222,22 +244,29 @@ static cudaError_t z_go(const InstT<T>* d, int ninst, int ntiles, const ZArgs& a
 // 128^2, ~157 KB at 192^2)
 #define CB_XYC_SIZES(X) X(64) X(96) X(128) X(192)
 
-template <class T> bool Launch<T>::xy_cluster_ok(int nx) {
+template <class T> bool Launch<T>::xy_cluster_ok(int nx, int curv) {
     switch (nx) {
-#define CASE(n) case n: return xyc_ok<T, n>();
+#define CASE(n) case n: return curv ? xyc_ok<T, n, 1>() : xyc_ok<T, n>();
         CB_XYC_SIZES(CASE)
 #undef CASE
         default: return false;
     }
 }
 
-template <class T> bool Launch<T>::xy_single(int nx, int nf) {
+template <class T> bool Launch<T>::xy_single(int nx, int nf, int curv) {
     switch (nx) {
-#define CASE(n) case n: return nf == 2 ? XYCfg<T, n>::ok : XYCfg<T, n>::ok1;
+#define CASE(n) case n: return nf == 2 ? (curv ? XYCfg<T, n>::ok_q : XYCfg<T, n>::ok) : XYCfg<T, n>::ok1;
         CB_XY_SIZES(CASE)
 #undef CASE
         default: return false;
     }
+}
+// the FP32 fused pass with curvature runs on the cluster or one-CTA plane kernels only
+// (the split passes carry no third field): true where `path` resolves to one of them
+template <class T> bool Launch<T>::fused_curv_ok(int nx, int path) {
+    if (sizeof(T) != 4 || path == XYP_SPLIT) return false;
+    if (path == XYP_CLUSTER && xy_cluster_ok(nx, 1)) return true;
+    return xy_single(nx, 2, 1);
 }
 template <class T> bool Launch<T>::xy_split_supported(int nx) {
     switch (nx) {
@@ -264,15 +293,23 @@ template <class T>
 cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const XYArgs& a, cudaStream_t s,
                           int path) {
     const int nf = (a.mode == XY_REDUCE_FULL || a.mode == XY_NONLIN || a.mode == XY_FUSED) ? 2 : 1;
-    if (path == XYP_CLUSTER && a.mode == XY_FUSED && xy_cluster_ok(nx)) {
+    const int curv = sizeof(T) == 4 && a.curv && a.mode == XY_FUSED;
+    if (path == XYP_CLUSTER && a.mode == XY_FUSED && xy_cluster_ok(nx, curv)) {
         switch (nx) {
-#define CASE(n) case n: if constexpr (xyc_ok<T, n>()) return xyc_go<T, n>(d, ninst, nzmax, a, s); break;
+#define CASE(n)                                                                                       \
+    case n:                                                                                           \
+        if (curv) {                                                                                   \
+            if constexpr (xyc_ok<T, n, 1>()) return xyc_go<T, n, 1>(d, ninst, nzmax, a, s);           \
+        } else {                                                                                      \
+            if constexpr (xyc_ok<T, n>()) return xyc_go<T, n>(d, ninst, nzmax, a, s);                 \
+        }                                                                                             \
+        break;
             CB_XYC_SIZES(CASE)
 #undef CASE
             default: break;
         }
     }
-    if (path != XYP_SPLIT && xy_single(nx, nf)) {
+    if (path != XYP_SPLIT && xy_single(nx, nf, curv)) {
         switch (nx) {
 #define CASE(n) case n: return xy_go<T, n>(d, ninst, nzmax, a, s, path != XYP_SINGLE);
             CB_XY_SIZES(CASE)
@@ -280,6 +317,7 @@ cudaError_t Launch<T>::xy(int nx, const InstT<T>* d, int ninst, int nzmax, const
             default: return cudaErrorInvalidValue;
         }
     }
+    if (curv) return cudaErrorInvalidValue;  // the split passes carry no third field (fused_curv_ok)
     switch (nx) {
 #define CASE(n) case n: return xy_split_go<T, n>(d, ninst, nzmax, a, s);
         CB_Z_SIZES(CASE)
@@ -335,9 +373,10 @@ cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_
 #define CB_INSTANTIATE_XY(T)                                                                                        \
     template bool cb::Launch<T>::xy_supported(int);                                                                 \
     template bool cb::Launch<T>::xy_plain_supported(int);                                                           \
-    template bool cb::Launch<T>::xy_single(int, int);                                                               \
+    template bool cb::Launch<T>::xy_single(int, int, int);                                                          \
     template bool cb::Launch<T>::xy_split_supported(int);                                                           \
-    template bool cb::Launch<T>::xy_cluster_ok(int);                                                                \
+    template bool cb::Launch<T>::xy_cluster_ok(int, int);                                                           \
+    template bool cb::Launch<T>::fused_curv_ok(int, int);                                                           \
     template int cb::Launch<T>::xy_rows_per_cta(int);                                                               \
     template cudaError_t cb::Launch<T>::xy(int, const cb::InstT<T>*, int, int, const cb::XYArgs&, cudaStream_t, int); \
     template cudaError_t cb::Launch<T>::decide(const cb::InstT<T>*, int, int, cudaStream_t);                        \

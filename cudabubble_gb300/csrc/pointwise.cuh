@@ -210,8 +210,16 @@ __device__ __forceinline__ void ff_add_f2(float4 U, float2 v, float2& uh, float2
 // sum carries S, whose error moves the area penalty's lambda2 and, through it,
 // the volume (a plain FP32 u^2 - 1 put ~1e-8 into S).  Otherwise as
 // fused_point<float>.
+//
+// With CURV (spontaneous curvature C, the reference's commented-out formulas,
+// phasefield.cpp:183-250) f gives way to fc = f + C (u^2 - 1) in the energy sum and in the
+// Euler partial, the curvature part of the variational derivative joins G'', and the third
+// output q = C (u^2 - 1) (Euler) or eps C (u^2 - 1) (ETD) carries the term whose Laplacian
+// enters N: it is transformed like H and takes H's spectral multiplier (beta cx |k|^2),
+// while H itself stays f (Euler) or w (ETD), the field the lambda2 term is rebuilt from.
+template <bool CURV = false>
 __device__ __forceinline__ void fused_point_u2(const PC<float>& k, bool euler, float2 uh, float2 ul, float2 lap,
-                                               Acc2& as, Acc2& af, float2& g, float2& h) {
+                                               Acc2& as, Acc2& af, float2& g, float2& h, float2* q = nullptr) {
     using namespace lane2;
     const float2 one = bc(1.f), mone = bc(-1.f);
     const float2 p = mul(uh, uh);
@@ -228,13 +236,30 @@ __device__ __forceinline__ void fused_point_u2(const PC<float>& k, bool euler, f
     const float2 w = mul(u2m, uh);
     const float2 f = sub(kmul(k.k_ieps, w), kmul(k.k_eps, lap));
     as.add(sq, lane2::add(fma(u2m, u2m, neg(sq)), mul(mul(bc(2.f), u2m), u2m_lo)));
-    af.add(mul(f, f), bc(0.f));
-    if (euler) {
-        g = kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), one), f));
-        h = f;
+    if constexpr (CURV) {
+        const float2 cu = mul(u2m, bc(k.C));
+        const float2 fc = lane2::add(f, cu);
+        af.add(mul(fc, fc), bc(0.f));
+        *q = mul(u2m, bc(k.qC));
+        const float2 t3 = sub(mul(bc(3.f), u2), one);  // 3 u^2 - 1
+        if (euler) {  // eta (3u^2 - 1 + 2 eps u C) fc / eps^2
+            g = kmul(k.k_K2, mul(lane2::add(t3, mul(bc(k.e2C), uh)), fc));
+            h = f;
+        } else {  // ... - eta ((3u^2 - 1) cu + 2 eps u C fc) / eps^2
+            g = neg(lane2::add(kmul(k.k_K3, w), kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), bc(2.5f)), f))));
+            g = sub(g, kmul(k.k_K2, lane2::add(mul(t3, cu), mul(mul(bc(k.e2C), uh), fc))));
+            h = w;
+        }
     } else {
-        g = neg(lane2::add(kmul(k.k_K3, w), kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), bc(2.5f)), f))));
-        h = w;
+        (void)q;
+        af.add(mul(f, f), bc(0.f));
+        if (euler) {
+            g = kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), one), f));
+            h = f;
+        } else {
+            g = neg(lane2::add(kmul(k.k_K3, w), kmul(k.k_K2, mul(sub(mul(bc(3.f), u2), bc(2.5f)), f))));
+            h = w;
+        }
     }
 }
 

@@ -64,7 +64,7 @@ __global__ void ellipsoid_kernel(double* __restrict__ out, int nx, int nz, doubl
 }
 
 template <class T> struct PoolClass {
-    int nx = 0, nz = 0, method = 0, accurate = 0, cap = 0, ntiles = 0, split = 0;
+    int nx = 0, nz = 0, method = 0, accurate = 0, cap = 0, ntiles = 0, split = 0, curv = 0;
     InstT<T>* table = nullptr;
     SlotSummary* sum = nullptr;
     std::vector<Stepper<T>*> occ;
@@ -101,19 +101,20 @@ template <class T> class Pool {
         return CB_OK;
     }
 
-    int find(int nx, int nz, int method, int accurate, int split) const {
+    int find(int nx, int nz, int method, int accurate, int split, int curv) const {
         for (size_t i = 0; i < cls.size(); ++i)
             if (cls[i].nx == nx && cls[i].nz == nz && cls[i].method == method && cls[i].accurate == accurate &&
-                cls[i].split == split)
+                cls[i].split == split && cls[i].curv == curv)
                 return (int)i;
         return -1;
     }
 
-    int add_class(int nx, int nz, int method, int accurate, int split, int ntiles, int cap) {
+    int add_class(int nx, int nz, int method, int accurate, int split, int curv, int ntiles, int cap) {
         if (g) return fail(CB_EINVAL, "pool graph already built");
         PoolClass<T> c;
         c.nx = nx; c.nz = nz; c.method = method; c.accurate = accurate; c.cap = cap; c.ntiles = ntiles;
         c.split = split;
+        c.curv = curv;
         c.occ.assign(cap, nullptr);
         CB_CK(cudaMalloc(&c.table, sizeof(InstT<T>) * cap));
         CB_CK(cudaMalloc(&c.sum, sizeof(SlotSummary) * cap));
@@ -129,7 +130,7 @@ template <class T> class Pool {
     // put an instance into a free slot of its class
     int place(Stepper<T>* sp, int* ci, int* si) {
         const Params& p = sp->params();
-        const int c = find(p.nx, p.nz, p.method, sp->accurate(), p.split);
+        const int c = find(p.nx, p.nz, p.method, sp->accurate(), p.split, p.curv);
         if (c < 0) return fail(CB_EINVAL, "no size class for %dx%dx%d", p.nx, p.ny, p.nz);
         for (int k = 0; k < cls[c].cap; ++k) {
             if (!cls[c].occ[k]) {
@@ -168,7 +169,8 @@ template <class T> class Pool {
             if (r == cudaSuccess) r = cudaEventRecord(c.fork, st);
             if (r == cudaSuccess) r = cudaStreamWaitEvent(c.s, c.fork, 0);
             if (r == cudaSuccess)
-                r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false, c.split, c.s);
+                r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false, c.split,
+                                     c.curv, c.s);
             if (r == cudaSuccess) r = cudaEventRecord(c.join, c.s);
             if (r == cudaSuccess) r = cudaStreamWaitEvent(st, c.join, 0);
         }
@@ -251,13 +253,15 @@ template <class T> class Batch final : public BatchBase {
         }
         for (auto& it : items) {
             const Params& p = it->params();
-            if (pool->find(p.nx, p.nz, p.method, it->accurate(), p.split) >= 0) continue;
+            if (pool->find(p.nx, p.nz, p.method, it->accurate(), p.split, p.curv) >= 0) continue;
             int cap = 0;
             for (auto& jt : items) {
                 const Params& q = jt->params();
-                if (q.nx == p.nx && q.nz == p.nz && q.method == p.method && jt->accurate() == it->accurate()) ++cap;
+                if (q.nx == p.nx && q.nz == p.nz && q.method == p.method && jt->accurate() == it->accurate() &&
+                    q.split == p.split && q.curv == p.curv)
+                    ++cap;
             }
-            rc = pool->add_class(p.nx, p.nz, p.method, it->accurate(), p.split, it->tiles(), cap);
+            rc = pool->add_class(p.nx, p.nz, p.method, it->accurate(), p.split, p.curv, it->tiles(), cap);
             if (rc) return rc;
         }
         where.resize(n);
@@ -418,7 +422,7 @@ class ArenaRegion {
 // so each class advances at its own pace (a 32^3 request is not paced by a 256^3
 // one), and its per-slot summaries copied back to pinned host memory.
 template <class T> struct ServeClass {
-    int nx = 0, nz = 0, method = 0, accurate = 0, split = 0, cap = 0, ntiles = 0, quantum = 1;
+    int nx = 0, nz = 0, method = 0, accurate = 0, split = 0, curv = 0, cap = 0, ntiles = 0, quantum = 1;
     long long bytes = 0;
     InstT<T>* table = nullptr;   // device slot table
     InstT<T>* h_table = nullptr; // pinned mirror, the source of the table's copies
@@ -469,7 +473,7 @@ template <class T> struct Server {
         for (size_t i = 0; i < cls.size(); ++i) {
             const auto& c = cls[i];
             if (c.nx == e.p.nx && c.nz == e.p.nz && c.method == e.p.method && c.accurate == e.accurate &&
-                c.split == e.p.split)
+                c.split == e.p.split && c.curv == e.p.curv)
                 return (int)i;
         }
         return -1;
@@ -496,6 +500,7 @@ template <class T> struct Server {
             if (find(e) >= 0) continue;
             ServeClass<T> c;
             c.nx = e.p.nx; c.nz = e.p.nz; c.method = e.p.method; c.accurate = e.accurate; c.split = e.p.split;
+            c.curv = e.p.curv;
             c.bytes = (long long)instance_arena_bytes<T>(e.p);
             if (c.bytes > budget) return fail(CB_ENOMEM, "request %d needs %lld bytes, over the budget", i, c.bytes);
             c.cap = (int)std::max<long long>(1, std::min<long long>(max_slots, budget / c.bytes));
@@ -541,7 +546,7 @@ template <class T> struct Server {
             cudaGraph_t gr = nullptr;
             CB_CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
             cudaError_t r = enqueue_group<T>(c.method, c.nx, c.nz, c.table, c.cap, c.ntiles, c.accurate, false,
-                                             c.split, c.s);
+                                             c.split, c.curv, c.s);
             cudaError_t ee = cudaStreamEndCapture(c.s, &gr);
             if (r != cudaSuccess || ee != cudaSuccess) {
                 if (gr) cudaGraphDestroy(gr);

@@ -129,8 +129,6 @@ inline int make_params(const cb_params& u, Eff& e) {
         return fail(CB_EINVAL, "grid %dx%dx%d: nx must be even and positive (Calc.cu:52-55)", u.nx, u.nx, u.nz);
     if (u.method < CB_EULER || u.method > CB_ETD4) return fail(CB_EINVAL, "unknown method %d", u.method);
     if (u.precision != CB_FP64 && u.precision != CB_FP32) return fail(CB_EINVAL, "unknown precision %d", u.precision);
-    if (u.spont_c != 0.0 && u.precision != CB_FP64)
-        return fail(CB_EUNSUPPORTED, "spontaneous curvature runs in the plain FP64 form (precision CB_FP64)");
     if (!std::isfinite(u.spont_c)) return fail(CB_EINVAL, "spontaneous curvature must be finite");
     p.nx = u.nx;
     p.ny = u.nx;  // Calc.cu:45-46
@@ -165,6 +163,11 @@ inline int make_params(const cb_params& u, Eff& e) {
     // (belastic.cpp:653-668); a positive reject_tol tolerates rises below reject_tol |E|
     p.reject_tol = u.reject_tol >= 0 ? u.reject_tol : 0.0;
     p.C = u.spont_c;
+    // FP32 form with curvature: the fused passes carry the third field q = (eps) C (u^2 - 1)
+    p.curv = (u.precision == CB_FP32 && u.spont_c != 0.0) ? 1 : 0;
+    p.f_C = (float)p.C;
+    p.f_qC = (float)((euler ? 1.0 : p.eps) * p.C);
+    p.f_2eC = (float)(2.0 * p.eps * p.C);
     // nonlinear term N-hat = A-hat + beta cx |k|^2 B-hat: beta = eta (Euler, -lap f in g0)
     // or -eta/eps (ETD, +lap t / eps in -eta NL)
     const double beta = euler ? p.eta : -p.eta / p.eps;
@@ -230,7 +233,7 @@ enum { K_XY_NONLIN = 0, K_XY_REDUCE_S = 1, K_XY_REDUCE_FULL = 2, K_Z_STAGE = 3, 
 // event pair brackets every launch and is appended as (kind, start, end).
 template <class T>
 inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, int ninst, int ntiles, int accurate,
-                                 int raw, int split, cudaStream_t s,
+                                 int raw, int split, int curv, cudaStream_t s,
                                  std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr) {
     cudaError_t r = cudaSuccess;
     auto timed = [&](int kind, auto&& fn) {
@@ -254,6 +257,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             a.mode = m;
             a.role = role;
             a.skip_if_stale = skip;
+            a.curv = curv;
             return Launch<T>::xy(nx, d, ninst, nz, a, s, split);
         });
     };
@@ -263,6 +267,7 @@ inline cudaError_t enqueue_group(int method, int nx, int nz, const InstT<T>* d, 
             memset(&a, 0, sizeof a);
             a.mode = m;
             a.role = role;
+            a.curv = curv;
             return Launch<T>::z(nz, d, ninst, ntiles, a, s);
         });
     };
@@ -349,7 +354,8 @@ template <class T> inline size_t instance_arena_bytes(const Params& p, size_t* l
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t fs = al(ns * 16), fp = al(ns * sizeof(T) * 2);
     // Nu, P x6, A, B (+ Na, Nb), then the split path's Y0, Y1, then the FP32 form's G slots
-    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0) + (sizeof(T) == 4 ? 4 : 0);
+    const int nplain = 9 + (p.method == M_ETD4 ? 2 : 0) + (uses_split<T>(p) ? 2 : 0) + (sizeof(T) == 4 ? 4 : 0) +
+                       (p.curv ? 3 : 0);  // curvature: q of the work stage and of both G slots
     // FP32 form: the state's and the candidate's real-space u, double-float
     const size_t fu = sizeof(T) == 4 ? al((size_t)p.N * 8) : 0;
     // FP32 form: the FP64 plain transforms of set/get phi need their own Y0, Y1
@@ -403,6 +409,10 @@ template <class T> class Stepper final : public Handle {
         if (!Launch<T>::xy_supported(p.nx) || !Launch<T>::z_supported(p.nz))
             return fail(CB_EUNSUPPORTED, "grid %dx%dx%d not built for %s", p.nx, p.ny, p.nz,
                         sizeof(T) == 4 ? "FP32" : "FP64");
+        if (p.curv && !Launch<T>::fused_curv_ok(p.nx, p.split))
+            return fail(CB_EUNSUPPORTED,
+                        "spontaneous curvature in the FP32 form runs on the cluster and one-CTA plane passes "
+                        "(planes up to 128^2, not the split passes); use CB_FP64 for %dx%d planes", p.nx, p.ny);
         ns = (size_t)p.nz * p.ny * p.nc;
         ntiles = (p.ny * p.nc + Launch<T>::z_tile() - 1) / Launch<T>::z_tile();
         size_t lay[9];
@@ -436,6 +446,11 @@ template <class T> class Stepper final : public Handle {
             for (int i = 0; i < 2; ++i) h.Y[i] = base + lay[6] + (nextf++) * fp;
         if (sizeof(T) == 4) {
             for (int i = 0; i < 4; ++i) h.G[i / 2][i % 2] = base + lay[6] + (nextf++) * fp;
+            if (p.curv) {
+                h.G[0][2] = base + lay[6] + (nextf++) * fp;
+                h.G[1][2] = base + lay[6] + (nextf++) * fp;
+                h.Q = base + lay[6] + (nextf++) * fp;
+            }
             const size_t fu = ((size_t)p.N * 8 + 255) & ~(size_t)255;
             for (int i = 0; i < 2; ++i) h.U[i] = base + lay[8] + i * fu;
         }
@@ -634,9 +649,9 @@ template <class T> class Stepper final : public Handle {
     // holds only where the handle was created for them
     bool path_ok(int path) const {
         switch (path) {
-            case XYP_SPLIT: return h.Y[0] != nullptr && Launch<T>::xy_split_supported(p.nx);
-            case XYP_SINGLE: return Launch<T>::xy_single(p.nx, 2);
-            case XYP_CLUSTER: return sizeof(T) == 4 && Launch<T>::xy_cluster_ok(p.nx);
+            case XYP_SPLIT: return !p.curv && h.Y[0] != nullptr && Launch<T>::xy_split_supported(p.nx);
+            case XYP_SINGLE: return Launch<T>::xy_single(p.nx, 2, p.curv);
+            case XYP_CLUSTER: return sizeof(T) == 4 && Launch<T>::xy_cluster_ok(p.nx, p.curv);
             default: return false;
         }
     }
@@ -1102,6 +1117,7 @@ template <class T> class Stepper final : public Handle {
         a.mode = mode;
         a.role = role;
         a.skip_if_stale = skip;
+        a.curv = p.curv;
         return Launch<T>::xy(p.nx, d, 1, p.nz, a, st, p.split);
     }
     cudaError_t zpass(int mode, int role) {
@@ -1109,6 +1125,7 @@ template <class T> class Stepper final : public Handle {
         memset(&a, 0, sizeof a);
         a.mode = mode;
         a.role = role;
+        a.curv = p.curv;
         return Launch<T>::z(p.nz, d, 1, ntiles, a, st);
     }
     // real double field -> spectrum (x 1/N), through the partial buffer `part`
@@ -1198,7 +1215,7 @@ template <class T> class Stepper final : public Handle {
     int enqueue_attempt(int raw, std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>>* prof = nullptr,
                         int method = -1) {
         cudaError_t r = enqueue_group<T>(method < 0 ? p.method : method, p.nx, p.nz, d, 1, ntiles, e.accurate, raw,
-                                         p.split, st, prof);
+                                         p.split, p.curv, st, prof);
         if (r != cudaSuccess) return fail(CB_ECUDA, "enqueue attempt: %s", cudaGetErrorString(r));
         return CB_OK;
     }

@@ -21,26 +21,32 @@
 
 namespace cb {
 
-template <int NX> struct XYC {
+// NQ = 1 (the FP32 form with spontaneous curvature): a third output field q, transformed
+// forward in a shared-memory region of its own ([NH][M + 1] in the x stage, [NY][MH + 1]
+// in the y stage) and exchanged in a round of its own, so the register-staged exchange of
+// the two main fields keeps its size
+template <int NX, int NQ = 0> struct XYC {
     static constexpr int M = NX / 2, NY = NX, NC = M + 1, MH = M / 2, NH = NY / 2;
     static constexpr int PY = 2 * MH + 1;  // y layout: [NY][field 0 | field 1 of own columns]
     static constexpr int PX = 2 * M + 1;   // x layout: [NH][field 0 | field 1 of all columns]
     static constexpr int SZ = (NY * PY > NH * PX) ? NY * PY : NH * PX;
+    static constexpr int QX = M + 1, QY = MH + 1;  // pitches of the q region
+    static constexpr int SQ = NQ ? ((NH * QX > NY * QY) ? NH * QX : NY * QY) : 0;
 };
-
-template <class T, int NX> constexpr size_t xyc_smem_bytes() {
-    using Q = XYC<NX>;
+template <class T, int NX, int NQ = 0> constexpr size_t xyc_smem_bytes() {
+    using Q = XYC<NX, NQ>;
     constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
-    return sizeof(cplx<T>) * ((size_t)Q::SZ + ntw * (Q::M + NX + NX)) + (32 * 4 + 2) * sizeof(double);
+    return sizeof(cplx<T>) * ((size_t)Q::SZ + Q::SQ + ntw * (Q::M + NX + NX)) + (32 * 4 + 2) * sizeof(double);
 }
 
-template <class T, int NX, int NT>
+template <class T, int NX, int NT, int NQ = 0>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     xyc_fused_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
     namespace cg = cooperative_groups;
     using C = cplx<T>;
-    using Q = XYC<NX>;
+    using Q = XYC<NX, NQ>;
     constexpr int M = Q::M, NY = Q::NY, NC = Q::NC, MH = Q::MH, NH = Q::NH, PY = Q::PY, PX = Q::PX;
+    constexpr int QX = Q::QX, QY = Q::QY;
     constexpr int ntw = sizeof(T) == 4 ? 2 : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CB_PDL_TRIGGER();
@@ -56,7 +62,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     // both CTAs of a cluster hold the same plane of the same instance: they leave together
     if (z >= p.nz) return;
     C* S = reinterpret_cast<C*>(smem_raw);
-    C* twM = S + Q::SZ;
+    C* Qb = S + Q::SZ;  // the q region (NQ = 1)
+    C* twM = Qb + Q::SQ;
     C* twN = twM + M;
     C* twY = twN + NX;
     C* twMl = twY + NY;  // lo parts (FP32)
@@ -183,12 +190,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             float2 uh, ul;
             ff_add_f2(Uv, dd, uh, ul);
             if (Uo) Uo[ui] = make_float4(uh.x, ul.x, uh.y, ul.y);
-            float2 g, h;
-            fused_point_u2(k, euler, uh, ul, ll, as2, af2, g, h);
+            float2 g, h, qv;
+            fused_point_u2<NQ == 1>(k, euler, uh, ul, ll, as2, af2, g, h, &qv);
             ag2.add(g);
             ah2.add(h);
             *pu = g;
             *pl = h;
+            if constexpr (NQ == 1) Qb[r * QX + qq] = qv;
         }
         as.v = as2.part();
         af.v = af2.part();
@@ -200,12 +208,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
         __syncthreads();
     }
 
-    // ---- x R2C: forward M-point FFT, post-processing
-    fft_lines_TN<M, false, NT, 2 * NH>(S, rows, 1, twM, twMl);
+    // ---- x R2C: forward M-point FFT, post-processing (two fields, or three with q)
+    constexpr int NFO = 2 + NQ;
+    const TripleRows<NH, PX, M, Q::SZ, QX> rows3;
+    auto xrow = [&](int l) { return NQ ? rows3(l) : rows(l); };
+    if constexpr (NQ == 1) fft_lines_TN<M, false, NT, 3 * NH>(S, rows3, 1, twM, twMl);
+    else fft_lines_TN<M, false, NT, 2 * NH>(S, rows, 1, twM, twMl);
     __syncthreads();
-    for (int it = tid; it < 2 * NH * (M / 2 + 1); it += NT) {
-        const int l = it % (2 * NH), kk = it / (2 * NH);
-        C* row = S + rows(l);
+    for (int it = tid; it < NFO * NH * (M / 2 + 1); it += NT) {
+        const int l = it % (NFO * NH), kk = it / (NFO * NH);
+        C* row = S + xrow(l);
         if (kk == 0) {
             const C z0 = row[0];
             row[0] = cmk<C>(z0.x + z0.y, z0.x - z0.y);  // X[0] + i X[M]
@@ -246,15 +258,45 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             S[s * PY + rem] = rg[e];
         }
     }
+    if constexpr (NQ == 1) {
+        // q: own columns of every row slot, from both CTAs' x-stage q regions (unchanged
+        // since the barriers above) into this CTA's y layout [NY][QY]
+        constexpr int NEQ = NY * MH, EPQ = (NEQ + NT - 1) / NT;
+        C rq[EPQ];
+        const C* Qp = cl.map_shared_rank(Qb, rank ^ 1);
+#pragma unroll
+        for (int e = 0; e < EPQ; ++e) {
+            const int idx = tid + e * NT;
+            if (idx < NEQ) {
+                const int s = idx / MH, cc = idx - s * MH, o = s / NH;
+                const C* src = o == rank ? Qb : Qp;
+                rq[e] = src[(s - o * NH) * QX + c0 + cc];
+            }
+        }
+        cl.sync();  // both CTAs have read their q before either rewrites its region
+#pragma unroll
+        for (int e = 0; e < EPQ; ++e) {
+            const int idx = tid + e * NT;
+            if (idx < NEQ) {
+                const int s = idx / MH, cc = idx - s * MH;
+                Qb[s * QY + cc] = rq[e];
+            }
+        }
+    }
     __syncthreads();
     fft_lines_TN<NY, false, NT, 2 * MH>(S, LinearLines{1}, PY, twY, twYl);
+    if constexpr (NQ == 1) {
+        __syncthreads();
+        fft_lines_TN<NY, false, NT, MH>(Qb, LinearLines{1}, QY, twY, twYl);
+    }
     __syncthreads();
 
     // ---- store own columns, unpacking the kx = 0 / nx/2 pair (rank 0)
-    void *oa, *ob;
-    nl_outputs<T>(I, ctrl, XY_FUSED, a.role, oa, ob);
+    void *oa, *ob, *oq;
+    nl_outputs<T>(I, ctrl, XY_FUSED, a.role, oa, ob, &oq);
     C* outA = reinterpret_cast<C*>(oa) + (size_t)z * plane;
     C* outB = reinterpret_cast<C*>(ob) + (size_t)z * plane;
+    C* outQ = NQ ? reinterpret_cast<C*>(oq) + (size_t)z * plane : nullptr;
     auto add_bnl = [&](C g, C hh, int kk) {
         if constexpr (sizeof(T) == 8) {
             const T mm = k.bnl * (T)kk;
@@ -275,12 +317,28 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             const C gN = cmk<C>(h * (zg.y + zg2.y), h * (zg2.x - zg.x));
             const C h0 = cmk<C>(h * (zh.x + zh2.x), h * (zh.y - zh2.y));
             const C hN = cmk<C>(h * (zh.y + zh2.y), h * (zh2.x - zh.x));
-            outA[ky * NC] = add_bnl(g0, h0, kyf * kyf);
-            outA[ky * NC + M] = add_bnl(gN, hN, M * M + kyf * kyf);
+            if constexpr (NQ == 1) {  // q takes H's multiplier: A = G + beta cx |k_xy|^2 (H + q)
+                const C zq = Qb[ky * QY], zq2 = Qb[kym * QY];
+                const C q0 = cmk<C>(h * (zq.x + zq2.x), h * (zq.y - zq2.y));
+                const C qN = cmk<C>(h * (zq.y + zq2.y), h * (zq2.x - zq.x));
+                outA[ky * NC] = add_bnl(g0, cadd(h0, q0), kyf * kyf);
+                outA[ky * NC + M] = add_bnl(gN, cadd(hN, qN), M * M + kyf * kyf);
+                outQ[ky * NC] = q0;
+                outQ[ky * NC + M] = qN;
+            } else {
+                outA[ky * NC] = add_bnl(g0, h0, kyf * kyf);
+                outA[ky * NC + M] = add_bnl(gN, hN, M * M + kyf * kyf);
+            }
             outB[ky * NC] = h0;
             outB[ky * NC + M] = hN;
         } else {
-            outA[ky * NC + c] = add_bnl(zg, zh, c * c + kyf * kyf);
+            if constexpr (NQ == 1) {
+                const C zq = Qb[ky * QY + cc];
+                outA[ky * NC + c] = add_bnl(zg, cadd(zh, zq), c * c + kyf * kyf);
+                outQ[ky * NC + c] = zq;
+            } else {
+                outA[ky * NC + c] = add_bnl(zg, zh, c * c + kyf * kyf);
+            }
             outB[ky * NC + c] = zh;
         }
     }

@@ -91,25 +91,32 @@ __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Par
 
 // where a nonlinear pass leaves its two forward-transformed fields: the work
 // pair A, B, or (XY_FUSED of the state / candidate) that role's G slot
+// (and, for the FP32 form with curvature, its third field q in *Qo)
 template <class T>
-__device__ __forceinline__ void nl_outputs(const InstT<T>& I, const Ctrl* c, int mode, int role, void*& A, void*& B) {
+__device__ __forceinline__ void nl_outputs(const InstT<T>& I, const Ctrl* c, int mode, int role, void*& A, void*& B,
+                                           void** Qo = nullptr) {
     if (mode == XY_FUSED && role != R_WORK) {
         const int sl = role == R_STATE ? c->ab_state : 1 - c->ab_state;
         A = I.G[sl][0];
         B = I.G[sl][1];
+        if (Qo) *Qo = I.G[sl][2];
     } else {
         A = I.A;
         B = I.B;
+        if (Qo) *Qo = I.Q;
     }
 }
 
-// NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN / XY_FUSED, 1 otherwise
-template <class T, int NX, int NT, int NF>
+// NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN / XY_FUSED, 1 otherwise.
+// NQ = 1: the FP32 fused pass with spontaneous curvature, whose third output field q lives
+// in a region of its own, [NY][M + 1] after the plane (pointwise.cuh, fused_point_u2)
+template <class T, int NX, int NT, int NF, int NQ = 0>
 __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
     using C = cplx<T>;
     constexpr int M = NX / 2, NY = NX, NC = M + 1;
     constexpr int nf = NF;
     constexpr int pitch = nf * M + 1;
+    constexpr int QX = M + 1, SQ = NQ ? NY * QX : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CB_PDL_TRIGGER();
     const InstT<T>& I = insts[blockIdx.y];
@@ -119,7 +126,8 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     const int tid = threadIdx.x;
     if (z >= p.nz) return;
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
-    C* twM = S + NY * pitch;                // W_M^m
+    C* Qb = S + NY * pitch;                 // q (NQ = 1)
+    C* twM = Qb + SQ;                       // W_M^m
     C* twN = twM + M;                       // W_NX^m
     C* twY = twN + NX;                      // W_NY^m
     // FP32: lo parts of the three tables (same order), FP64: unused aliases
@@ -318,12 +326,13 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                     float2 uh, ul;
                     ff_add_f2(Uv, dd, uh, ul);
                     if (Uo) Uo[ui] = make_float4(uh.x, ul.x, uh.y, ul.y);
-                    float2 g, h;
-                    fused_point_u2(k, euler, uh, ul, ll, as2, af2, g, h);
+                    float2 g, h, qv;
+                    fused_point_u2<NQ == 1>(k, euler, uh, ul, ll, as2, af2, g, h, &qv);
                     ag2.add(g);
                     ah2.add(h);
                     *pu = g;
                     *pl = h;
+                    if constexpr (NQ == 1) Qb[r * QX + q] = qv;
                 }
                 as.v = as2.part();
                 af.v = af2.part();
@@ -367,13 +376,16 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     }
 
     // ---- forward xy: x R2C (transposed in, natural out) then y (transposed in, natural out)
-    constexpr int nfo = NF;  // XY_NONLIN / XY_FUSED (2 fields) or XY_FWD_PLAIN (1)
+    constexpr int nfo = NF + NQ;  // XY_NONLIN / XY_FUSED (2 fields, 3 with q) or XY_FWD_PLAIN (1)
     const PairRows<NY, pitch, M> rows;
-    fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl);
+    const TripleRows<NY, pitch, M, NY * pitch, QX> rows3;
+    auto xrow = [&](int l) { return NQ ? rows3(l) : rows(l); };
+    if constexpr (NQ == 1) fft_lines_TN<M, false, NT, 3 * NY>(S, rows3, 1, twM, twMl);
+    else fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl);
     __syncthreads();
     for (int it = tid; it < nfo * NY * (M / 2 + 1); it += NT) {
         const int l = it % (nfo * NY), k = it / (nfo * NY);
-        C* row = S + rows(l);
+        C* row = S + xrow(l);
         if (k == 0) {
             const C z0 = row[0];
             row[0] = cmk<C>(z0.x + z0.y, z0.x - z0.y);  // X[0] + i X[M]
@@ -394,17 +406,23 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         }
     }
     __syncthreads();
-    fft_lines_TN<NY, false, NT, nfo * M>(S, LinearLines{1}, pitch, twY, twYl);
+    fft_lines_TN<NY, false, NT, NF * M>(S, LinearLines{1}, pitch, twY, twYl);
+    if constexpr (NQ == 1) {
+        __syncthreads();
+        fft_lines_TN<NY, false, NT, M>(Qb, LinearLines{1}, QX, twY, twYl);
+    }
     __syncthreads();
 
     // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
     C* outA;
     C* outB = nullptr;
+    C* outQ = nullptr;
     if (a.mode == XY_NONLIN || a.mode == XY_FUSED) {
-        void *oa, *ob;
-        nl_outputs<T>(I, ctrl, a.mode, a.role, oa, ob);
+        void *oa, *ob, *oq;
+        nl_outputs<T>(I, ctrl, a.mode, a.role, oa, ob, &oq);
         outA = reinterpret_cast<C*>(oa) + (size_t)z * plane;
         outB = reinterpret_cast<C*>(ob) + (size_t)z * plane;
+        if constexpr (NQ == 1) outQ = reinterpret_cast<C*>(oq) + (size_t)z * plane;
     } else {
         outA = reinterpret_cast<C*>(a.cout) + (size_t)z * plane;
     }
@@ -432,8 +450,18 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
                 const C zh = S[ky * pitch + M], zh2 = S[kym * pitch + M];
                 const C h0 = cmk<C>(h * (zh.x + zh2.x), h * (zh.y - zh2.y));
                 const C hN = cmk<C>(h * (zh.y + zh2.y), h * (zh2.x - zh.x));
-                outA[ky * NC] = add_bnl(g0, h0, kyf * kyf);
-                outA[ky * NC + M] = add_bnl(gN, hN, M * M + kyf * kyf);
+                if constexpr (NQ == 1) {  // q takes H's multiplier: A = G + beta cx |k_xy|^2 (H + q)
+                    const C zq = Qb[ky * QX], zq2 = Qb[kym * QX];
+                    const C q0 = cmk<C>(h * (zq.x + zq2.x), h * (zq.y - zq2.y));
+                    const C qN = cmk<C>(h * (zq.y + zq2.y), h * (zq2.x - zq.x));
+                    outA[ky * NC] = add_bnl(g0, cadd(h0, q0), kyf * kyf);
+                    outA[ky * NC + M] = add_bnl(gN, cadd(hN, qN), M * M + kyf * kyf);
+                    outQ[ky * NC] = q0;
+                    outQ[ky * NC + M] = qN;
+                } else {
+                    outA[ky * NC] = add_bnl(g0, h0, kyf * kyf);
+                    outA[ky * NC + M] = add_bnl(gN, hN, M * M + kyf * kyf);
+                }
                 outB[ky * NC] = h0;
                 outB[ky * NC + M] = hN;
             } else {
@@ -443,7 +471,13 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
         } else {
             if (outB) {
                 const C zh = S[ky * pitch + M + c];
-                outA[ky * NC + c] = add_bnl(zg, zh, c * c + kyf * kyf);
+                if constexpr (NQ == 1) {
+                    const C zq = Qb[ky * QX + c];
+                    outA[ky * NC + c] = add_bnl(zg, cadd(zh, zq), c * c + kyf * kyf);
+                    outQ[ky * NC + c] = zq;
+                } else {
+                    outA[ky * NC + c] = add_bnl(zg, zh, c * c + kyf * kyf);
+                }
                 outB[ky * NC + c] = zh;
             } else {
                 outA[ky * NC + c] = zg;
@@ -452,9 +486,10 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     }
 }
 
-template <class T, int NX> constexpr size_t xy_smem_bytes(int nf) {
+template <class T, int NX> constexpr size_t xy_smem_bytes(int nf, int nq = 0) {
     constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
-    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + ntw * (NX / 2 + NX + NX)) +
+    return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + (nq ? (size_t)NX * (NX / 2 + 1) : 0) +
+                              ntw * (NX / 2 + NX + NX)) +
            (32 * 4 + 2) * sizeof(double);
 }
 

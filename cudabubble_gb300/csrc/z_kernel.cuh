@@ -130,7 +130,10 @@ __host__ __device__ constexpr int zgroup_of(int mode) {
          : mode == Z_EULER ? ZG_EULER : ZG_PLAIN;
 }
 
-template <class T, int NZ, int TX, int NT, int MG>
+// NQ = 1 (FP32 stage groups with spontaneous curvature): the stage's third partial q is
+// transformed with A and B and takes B's multiplier, N-hat = (A-hat + beta cx kz^2 (B-hat +
+// q-hat)) / N, while f-hat keeps being rebuilt from B-hat alone
+template <class T, int NZ, int TX, int NT, int MG, int NQ = 0>
 __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
@@ -146,9 +149,10 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     if (m0 >= Mc) return;
     const void* g_a[2] = {I.G[0][0], I.G[1][0]};
     const void* g_b[2] = {I.G[0][1], I.G[1][1]};
+    const void* g_q[2] = {I.G[0][2], I.G[1][2]};
     const bool plain = a.mode == Z_FWD_PLAIN || a.mode == Z_INV_PLAIN;
     const int ntiles = (Mc + TX - 1) / TX;
-    constexpr int W = 2 * TX;  // row pitch: field 0 in [0, TX), field 1 in [TX, 2 TX)
+    constexpr int W = (2 + NQ) * TX;  // row pitch: field 0 in [0, TX), field 1 in [TX, 2 TX), q after
     C* S = reinterpret_cast<C*>(smem_raw);
     C* tw = S + NZ * W;
     constexpr int ntw = sizeof(T) == 4 ? 2 : 1;  // FP32: hi table then lo table
@@ -196,29 +200,33 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
         // stage 1 of the FP32 form reads the state's fused-pass outputs (G slot)
         const void* srcA = I.A;
         const void* srcB = I.B;
+        const void* srcQ = I.Q;
         if constexpr (sizeof(T) == 4) {
             if (stage1) {
                 srcA = c_ab ? g_a[1] : g_a[0];
                 srcB = c_ab ? g_b[1] : g_b[0];
+                srcQ = c_ab ? g_q[1] : g_q[0];
             }
         }
         const C* gA = reinterpret_cast<const C*>(a.mode == Z_FWD_PLAIN ? a.cin : srcA);
         const C* gB = reinterpret_cast<const C*>(srcB);
+        const C* gQ = reinterpret_cast<const C*>(srcQ);
         const bool two = a.mode != Z_FWD_PLAIN;
         // batches of LB loads per thread in flight before the shared-memory stores
         constexpr int LB = 4;
         constexpr int ITER = (NZ * TX + NT - 1) / NT;
         for (int b0 = 0; b0 < ITER; b0 += LB) {
-            C va[LB], vb[LB];
+            C va[LB], vb[LB], vq[LB];
 #pragma unroll
             for (int j = 0; j < LB; ++j) {
                 const int it = tid + (b0 + j) * NT;
-                va[j] = vb[j] = cmk<C>(0, 0);
+                va[j] = vb[j] = vq[j] = cmk<C>(0, 0);
                 const int m = m0 + it % TX;
                 if (b0 + j < ITER && it < NZ * TX && m < Mc) {
                     const size_t gi = (size_t)(it / TX) * Mc + m;
                     va[j] = __ldg(gA + gi);
                     if (two) vb[j] = __ldg(gB + gi);
+                    if constexpr (NQ == 1) vq[j] = __ldg(gQ + gi);
                 }
             }
 #pragma unroll
@@ -228,6 +236,7 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
                     const int c = it % TX, zz = it / TX;
                     S[zz * W + c] = va[j];
                     S[zz * W + TX + c] = vb[j];
+                    if constexpr (NQ == 1) S[zz * W + 2 * TX + c] = vq[j];
                 }
             }
         }
@@ -296,7 +305,9 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
                 nh = cmk<C>((va.x + mz * vb.x) * invN, (va.y + mz * vb.y) * invN);
             } else {  // beta cx and 1/N folded hi + lo: no systematic gain on N-hat
                 const T kk = (T)(kzf * kzf);
-                nh = cmk<C>(k.k_invN.mul(va.x + k.k_bnl.mul(kk * vb.x)), k.k_invN.mul(va.y + k.k_bnl.mul(kk * vb.y)));
+                C vm = vb;  // the field under the multiplier: B, or B + q with curvature
+                if constexpr (NQ == 1) vm = cadd(vb, S[r * W + 2 * TX + c]);
+                nh = cmk<C>(k.k_invN.mul(va.x + k.k_bnl.mul(kk * vm.x)), k.k_invN.mul(va.y + k.k_bnl.mul(kk * vm.y)));
                 wn = cmk<C>(k.k_invN.mul(vb.x), k.k_invN.mul(vb.y));
             }
         }
@@ -547,7 +558,7 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     }
     __syncthreads();
     const bool two = a.mode != Z_INV_PLAIN;
-    if (two) fft_lines_TN<NZ, true, NT, W>(S, LinearLines{1}, W, tw, twl);
+    if (two) fft_lines_TN<NZ, true, NT, 2 * TX>(S, LinearLines{1}, W, tw, twl);
     else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw, twl);
     __syncthreads();
 
@@ -598,9 +609,9 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     }
 }
 
-template <class T, int NZ, int TX> constexpr size_t z_smem_bytes() {
+template <class T, int NZ, int TX, int NQ = 0> constexpr size_t z_smem_bytes() {
     constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
-    return sizeof(cplx<T>) * ((size_t)NZ * 2 * TX + ntw * NZ) + (32 * 2 + 2) * sizeof(double);
+    return sizeof(cplx<T>) * ((size_t)NZ * (2 + NQ) * TX + ntw * NZ) + (32 * 2 + 2) * sizeof(double);
 }
 
 }  // namespace cb

@@ -102,7 +102,9 @@ typedef struct cb_params {
                                 < 0: default 0, the reference rule (belastic.cpp:653-668), for both forms */
     double spont_c;          /* spontaneous curvature C of fc = f + (phi^2 - 1) C, from the reference's
                                 commented-out formulas (phasefield.cpp:183-250); 0 (the reference, whose
-                                curvature field is NULL, fluidbase.cpp:150) or, in CB_FP64 only, any value */
+                                curvature field is NULL, fluidbase.cpp:150) or any value: CB_FP64 on every
+                                grid, CB_FP32 where the plane passes run as clusters or one CTA per plane
+                                (planes up to 128^2; the split passes return CB_EUNSUPPORTED) */
 } cb_params;
 
 typedef struct cb_scalars {
