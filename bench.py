@@ -21,9 +21,15 @@ Besides the headline line's keys, the JSON carries (unless --no-extra):
               "vs plain FP64" of the metric), and the FP32 form's speed-up;
   batched     workload config 4: 64 vesicles of grids drawn from
               {32,48,64,96,128}^3 advanced together (cb_batch_*);
-  served      workload config 5: a Poisson trace at 200 req/s of relaxations
-              on grids {32..256}^3 through the continuous-batching server
-              (cb_serve_trace), with p50/p99 latency.
+  served      workload config 5: the first 0.2 s of a Poisson trace at 200 req/s
+              of relaxations to |dE/E| < 1e-8 on grids {32..256}^3 through the
+              continuous-batching server (cb_serve_trace), run to completion, with
+              p50/p99 latency overall and per grid size;
+  ref_cufft   the reference's own FP64 cuFFT build (oracle/_ref/refstep, built by
+              build() from the staged sources) on the same workload and GPU;
+and (unless --no-cpu-baseline) cpu_baseline: the C port on the host cores, OpenMP and
+single-threaded.  The JSON line's `config` is the workload's identity and is the same
+in the --impl reference line; run details are under `run`.
 """
 from __future__ import annotations
 
@@ -50,6 +56,13 @@ UNIT = "grid-pt·steps/s"
 FLUSH_BYTES = 256 << 20
 WORKLOAD = ("C2: 128^3 periodic [-pi,pi]^3, seeded ellipsoid phi0 (seed 2), eps=1.5h, M1=M2=1e4, "
             "ETD-RK2, adaptive dt from 1e-6 (halve on energy rise, x2 every 4 steps, cap 1e-3), steps 1..K from phi0")
+
+
+def workload_config() -> dict:
+    """The workload's identity, the same in both arms' JSON lines (run details such as
+    attempts or the xy path go to `run`)."""
+    return {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2", "points": N_GRID ** 3,
+            "l2": "GPU arm: flushed between attempts (256 MiB memset, outside timed events)"}
 
 
 def phi0():
@@ -432,10 +445,9 @@ def run_ours(args, rank: int, world: int):
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
            "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 (FFT + pointwise), f64 reductions / scalars / energy test", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2", "attempts": attempts,
-                      "rejects": rejects, "l2": "flushed between attempts (256 MiB memset, outside timed events)",
-                      "parallelism": "replicas" if world > 1 else "single GPU", "points": N,
-                      **xy_path_config(tune)},
+           "config": workload_config(),
+           "run": {"attempts": attempts, "rejects": rejects,
+                   "parallelism": "replicas" if world > 1 else "single GPU", **xy_path_config(tune)},
            "accuracy": {"E_step_K": sc["E"], "E_reference_fp64_cufft": ref_E, "rel_E_error": rel_E},
            "e2e": e2e, "gpu_launches": attempts * LAUNCHES_PER_ATTEMPT, "roofline": roofline,
            "wall_s_timed_region": wall}
@@ -467,8 +479,9 @@ def main():
         res = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": r["steps"],
                "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": {"workload": WORKLOAD, "grid": [N_GRID] * 3, "method": "ETD-RK2",
-                          "note": "steps capped at 20 per run to bound CPU time"},
+               "config": workload_config(),
+               "run": {"attempts": None, "note": "steps capped at 20 per run to bound CPU time",
+                       "parallelism": f"OpenMP, {r['threads']} host threads"},
                "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["threads"], "kind": "port",
                                 "sample": f"steps 1..{r['steps']} of the workload (oracle/cstep.c, FP64, OpenMP on "
                                           f"{r['threads']} of {cores} host threads)"},
