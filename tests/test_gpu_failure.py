@@ -85,3 +85,49 @@ def test_launch_limit_times_out_and_resumes(cblib, prec):
     assert s["E"] == s_ref["E"] and s["dt"] == s_ref["dt"]
     assert np.array_equal(st.get_phi(), phi_ref)
     st.close()
+
+
+def test_nan_instance_in_a_batch_leaves_the_others_alone(cblib):
+    """One instance of a batch starts from a phi with a NaN: it alone ends with
+    CB_DONE_NONFINITE, and every other instance ends exactly as it does alone."""
+    from cudabubble_gb300 import capi
+    sizes = [32, 32, 48]
+    plist = [capi.default_params(nx=n, ny=n, nz=n, epssize=150, method=capi.CB_ETD2, precision=capi.CB_FP32,
+                                 time_step=1e-6) for n in sizes]
+    phis = [_phi0(n, seed=2 + i) for i, n in enumerate(sizes)]
+    bad = phis[1].copy()
+    bad[16, 16, 16] = np.nan
+    b = capi.Batch(plist)
+    for i, ph in enumerate(phis):
+        b.set_phi(i, bad if i == 1 else ph)
+    b.run(8)
+    assert b.scalars(1)["status"] == capi.CB_DONE_NONFINITE
+    for i in (0, 2):
+        st = capi.Stepper(plist[i])
+        st.set_phi(phis[i])
+        st.run(8)
+        assert np.array_equal(st.get_phi(), b.get_phi(i)), i
+        assert b.scalars(i)["status"] == capi.CB_DONE_TARGET
+        st.close()
+    b.close()
+
+
+def test_served_request_that_blows_up_ends_alone(cblib):
+    """A request whose shape is not a number (its phi0 is NaN everywhere) ends with
+    CB_DONE_NONFINITE at its first attempt; the requests beside it finish as usual."""
+    from cudabubble_gb300 import capi
+    reqs = []
+    for i, ax in enumerate(([1.6, 1.4, 0.9], [float("nan"), 1.4, 0.9], [1.5, 1.5, 1.0])):
+        rq = capi.cb_request()
+        rq.params = capi.default_params(nx=32, ny=32, nz=32, epssize=150, method=capi.CB_ETD2,
+                                        precision=capi.CB_FP32, time_step=1e-6, rel_tol=1e-6)
+        rq.axes[:] = ax
+        rq.arrival_s = 0.001 * i
+        rq.max_steps = 200
+        reqs.append(rq)
+    res, stats, _ = capi.serve_trace(reqs, 10 ** 10, max_slots_per_class=4, quantum=2)
+    assert stats["completed"] == 3
+    assert res[1]["status"] == capi.CB_DONE_NONFINITE and res[1]["steps"] == 0
+    for i in (0, 2):
+        assert res[i]["status"] in (capi.CB_DONE_TARGET, capi.CB_DONE_CONVERGED)
+        assert res[i]["steps"] > 0
