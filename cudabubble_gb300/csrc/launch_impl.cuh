@@ -14,6 +14,7 @@ namespace cb {
 
 constexpr size_t kMaxSmem = 227 * 1024;
 
+// [launch_k definition]
 // Launch with programmatic stream serialisation: the kernel's CTAs may be scheduled
 // while the previous kernel in the stream still runs, and wait in CB_PDL_WAIT for its
 // results (cb_fft.cuh).  Captured into a graph, the launch becomes a programmatic edge.
@@ -38,6 +39,7 @@ static cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_
 #endif
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
+// [end launch_k definition]
 
 // threads of the single-CTA xy pass for planes of 96^2 and 128^2: the
 // nonlinear pass (two fields both ways) gains from 32 warps per plane, the

@@ -664,34 +664,47 @@ template <class T> class Stepper final : public Handle {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         if (attempts < 1) return fail(CB_EINVAL, "attempts must be positive");
         CB_CK(pull());
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            if (e0) cudaEventDestroy(e0);
+            return fail(CB_ECUDA, "autotune: event creation failed");
+        }
         const Ctrl saved = hc;
         hc.target = INT_MAX;
         hc.done = 0;
         hc.fresh = 1;
-        CB_CK(push());
         const int keep = p.split;
         const int cands[3] = {XYP_CLUSTER, XYP_SINGLE, XYP_SPLIT};
         cb_tune_result r{};
         r.path = -1;
         double best = 1e300;
-        cudaEvent_t e0, e1;
-        CB_CK(cudaEventCreate(&e0));
-        CB_CK(cudaEventCreate(&e1));
         int rc = CB_OK;
+        {
+            const cudaError_t e = push();
+            if (e != cudaSuccess) rc = fail(CB_ECUDA, "autotune: push failed: %s", cudaGetErrorString(e));
+        }
+        // every error in the loop ends it through the restore below (path, control state,
+        // events, cached graphs), not by an early return
+        auto ck = [&](cudaError_t e, const char* what) {
+            if (e != cudaSuccess && rc == CB_OK) rc = fail(CB_ECUDA, "autotune: %s failed: %s", what, cudaGetErrorString(e));
+            return rc == CB_OK;
+        };
         for (int path : cands) {
+            if (rc) break;
             if (!path_ok(path)) continue;
             p.split = path;
             cudaGraphExec_t g = nullptr;
             rc = capture(2, &g);
             if (rc) break;
-            for (int i = 0; i < 2; ++i) CB_CK(cudaGraphLaunch(g, st));  // warm-up
-            CB_CK(cudaEventRecord(e0, st));
-            for (int i = 0; i < attempts; ++i) CB_CK(cudaGraphLaunch(g, st));
-            CB_CK(cudaEventRecord(e1, st));
-            CB_CK(cudaEventSynchronize(e1));
+            bool ok = true;
+            for (int i = 0; ok && i < 2; ++i) ok = ck(cudaGraphLaunch(g, st), "warm-up launch");
+            ok = ok && ck(cudaEventRecord(e0, st), "event record");
+            for (int i = 0; ok && i < attempts; ++i) ok = ck(cudaGraphLaunch(g, st), "timed launch");
+            ok = ok && ck(cudaEventRecord(e1, st), "event record") && ck(cudaEventSynchronize(e1), "event sync");
             float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
+            if (ok) ck(cudaEventElapsedTime(&ms, e0, e1), "elapsed time");
             cudaGraphExecDestroy(g);
+            if (rc) break;
             const double per = ms / attempts;
             r.paths[r.npaths] = path;
             r.ms_per_attempt[r.npaths] = per;
@@ -710,9 +723,11 @@ template <class T> class Stepper final : public Handle {
                 *gp = nullptr;
             }
         hc = saved;
-        CB_CK(push());
-        CB_CK(cudaStreamSynchronize(st));
+        const cudaError_t pe = push();
+        const cudaError_t se = cudaStreamSynchronize(st);
         if (rc) return rc;
+        CB_CK(pe);
+        CB_CK(se);
         if (r.npaths == 0) return fail(CB_EUNSUPPORTED, "no xy path to time");
         if (out) *out = r;
         return CB_OK;

@@ -3,8 +3,9 @@ emulation in tests/emu (used by tests/test_kernel_emulation.py and
 tests/test_host_emulation.py).
 
 - The dynamic shared-memory declaration becomes the emulated block's buffer.
-- Every ``kernel<<<grid, block, smem, stream>>>(args);`` launch becomes a call of
-  ``emu::launch_kernel`` with the same configuration and a closure running the kernel.
+- Every ``kernel<<<grid, block, smem, stream>>>(args);`` launch, and every call of the
+  ``launch_k`` helper, becomes a call of ``emu::launch_kernel`` with the same
+  configuration and a closure running the kernel.
 - The size lists of the launch dispatch shrink to the sizes a test builds.
 """
 import os
@@ -60,6 +61,37 @@ def rewrite_launches(text):
         i = m + 1
 
 
+def rewrite_launch_k(text):
+    """``launch_k(kernel, grid, block, smem, stream, args...)`` (the programmatic-launch
+    helper of launch_impl.cuh) becomes the same ``emu::launch_kernel`` call as a
+    triple-chevron launch; the helper's own definition is left alone."""
+    out, i = "", 0
+    while True:
+        j = text.find("launch_k(", i)
+        if j < 0:
+            return out + text[i:]
+        if text[max(0, j - 1)].isalnum() or text[max(0, j - 1)] == "_" or text[j:j + 22].startswith(
+                "launch_k(void (*kern)"):
+            out += text[i:j + 9]
+            i = j + 9
+            continue
+        depth, m = 0, j + 8
+        while True:
+            if text[m] == "(":
+                depth += 1
+            elif text[m] == ")":
+                depth -= 1
+                if depth == 0:
+                    break
+            m += 1
+        parts = _split_top(text[j + 9:m])
+        name, grid, block, smem, strm, args = parts[0], parts[1], parts[2], parts[3], parts[4], parts[5:]
+        clus = 2 if "xyc_fused_kernel" in name else 1
+        out += (text[i:j] + f"::emu::launch_kernel({grid}, {block}, (size_t)({smem}), (cudaStream_t)({strm}), "
+                f"(const void*)(&{name}), {clus}, [=]() {{ {name}({', '.join(args)}); }})")
+        i = m + 1
+
+
 def copy_sources(csrc, out, sizes=None, launches=False):
     """Copies csrc/*.cu, *.cuh, *.h to out with the rewrites; returns how many
     shared-memory declarations were rewritten."""
@@ -77,6 +109,10 @@ def copy_sources(csrc, out, sizes=None, launches=False):
                 t = re.sub(rf"#define {lst}\(X\).*", f"#define {lst}(X) {xs}", t)
         if launches and "<<<" in t:
             t = rewrite_launches(t)
+        if launches and "launch_k(" in t:
+            # the helper's definition goes (every call of it becomes an emulated launch)
+            t = re.sub(r"// \[launch_k definition\].*?// \[end launch_k definition\]", "", t, flags=re.S)
+            t = rewrite_launch_k(t)
         with open(os.path.join(out, f), "w") as fh:
             fh.write(t)
     return n_decl
