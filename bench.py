@@ -11,7 +11,7 @@ the stepper's stream and L2 is flushed (256 MiB memset) between attempts,
 outside the timed events.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--no-cpu-baseline] [--no-extra]
+                  [--no-cpu-baseline] [--no-extra] [--only batched|served]
 
 --impl reference times the reference algorithm's CPU form (oracle/cstep.c,
 the plain FP64 C port with OpenMP on every host core) on the same workload.
@@ -464,6 +464,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--only", choices=["batched", "served"], default=None,
+                    help="run one extra workload alone and print its JSON (for profiling it)")
     ap.add_argument("--tune", action="store_true", help="choose xy paths with cb_autotune (default: size rule)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -489,6 +491,14 @@ def main():
         print(json.dumps(res))
         return
 
+    if args.only:  # one extra workload alone, e.g. under a profiler
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            r = batched(min(args.steps, 60), args.tune) if args.only == "batched" else \
+                served(SERVE_TRACE_S, SERVE_MAX_STEPS, args.tune)
+            print(json.dumps({"only": args.only, args.only: r}))
+        return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
