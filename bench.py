@@ -425,21 +425,24 @@ def run_ours(args, rank: int, world: int):
                                    "achieved_gbs": round(v["achieved_gbs"], 1),
                                    "share": round(v["ms_total"] / total_ms, 3)} for k, v in kern.items()}}
 
-    # end to end through the C ABI with host buffers: set_phi(host) + run(K) + get_phi(host)
+    # end to end through the C ABI with host buffers in pinned memory:
+    # set_phi(host) + run(K) + get_phi(host)
+    pin_in = torch.from_numpy(p0).pin_memory()
+    pin_out = torch.empty(p0.shape, dtype=torch.float64).pin_memory()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    st.set_phi(p0)
+    st.set_phi(pin_in.numpy())
     rr = st.run(args.steps)
-    out = st.get_phi()
+    out = st.get_phi(out=pin_out.numpy())
     sc2 = st.scalars()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_steps = sc2["steps"]
     e2e = {"value": job_throughput(N, e2e_steps, e2e_s, world), "unit": UNIT,
            "h2d_bytes_per_step": int(p0.nbytes / max(e2e_steps, 1)),
            "d2h_bytes_per_step": int((out.nbytes + 120) / max(e2e_steps, 1)),
-           "what": "cb_set_phi(host phi0) + cb_run(K) + cb_get_phi(host) + cb_scalars_get, wall clock"}
+           "what": "cb_set_phi(pinned host phi0) + cb_run(K) + cb_get_phi(pinned host) + cb_scalars_get, wall clock"}
     st.close()
 
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,

@@ -227,8 +227,12 @@ class Stepper:
         assert a.shape == self.shape, (a.shape, self.shape)
         check(lib().cb_set_phi(self.h, _dptr(a), 0))
 
-    def get_phi(self) -> np.ndarray:
-        out = np.empty(self.shape, np.float64)
+    def get_phi(self, out: np.ndarray | None = None) -> np.ndarray:
+        """phi in the .out layout; into `out` (C-contiguous float64, e.g. a pinned buffer)
+        when given."""
+        if out is None:
+            out = np.empty(self.shape, np.float64)
+        assert out.shape == self.shape and out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
         check(lib().cb_get_phi(self.h, _dptr(out), 0))
         return out
 
