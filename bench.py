@@ -11,7 +11,7 @@ the stepper's stream and L2 is flushed (256 MiB memset) between attempts,
 outside the timed events.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--no-cpu-baseline] [--no-extra] [--only batched|served]
+                  [--no-cpu-baseline] [--no-extra] [--only batched|batched_persistent|served]
 
 --impl reference times the reference algorithm's CPU form (oracle/cstep.c,
 the plain FP64 C port with OpenMP on every host core) on the same workload.
@@ -20,7 +20,10 @@ Besides the headline line's keys, the JSON carries (unless --no-extra):
   plain_fp64  the plain FP64 form of this stepper on the same workload (the
               "vs plain FP64" of the metric), and the FP32 form's speed-up;
   batched     workload config 4: 64 vesicles of grids drawn from
-              {32,48,64,96,128}^3 advanced together (cb_batch_*);
+              {32,48,64,96,128}^3 advanced together (cb_batch_*), a launch per
+              pass and grid size in one CUDA graph per attempt;
+  batched_persistent  the same workload through one persistent kernel per attempt
+              (CB_BATCH_PERSISTENT);
   served      workload config 5: the first 0.2 s of a Poisson trace at 200 req/s
               of relaxations to |dE/E| < 1e-8 on grids {32..256}^3 through the
               continuous-batching server (cb_serve_trace), run to completion, with
@@ -259,9 +262,10 @@ def plain_fp64(steps: int):
 PATH_NAMES = ["auto", "split", "single", "cluster"]
 
 
-def batched(steps: int, tune: bool = False):
+def batched(steps: int, tune: bool = False, persistent: bool = False):
     """Workload config 4 through cb_batch (FP32 form); with `tune`, the xy path of each
-    size class is chosen by cb_autotune first, else by the size rule."""
+    size class is chosen by cb_autotune first, else by the size rule; `persistent`: one
+    persistent kernel per attempt of every instance (CB_BATCH_PERSISTENT)."""
     from cudabubble_gb300 import capi, workloads
     plist, phis = workloads.batched()
     tuned = {}
@@ -270,7 +274,7 @@ def batched(steps: int, tune: bool = False):
         for p, ph in zip(plist, phis):
             first.setdefault((p.nx, p.nz, p.method, p.precision), ph)
         tuned = capi.tune_xy_paths(plist, lambda p: first[(p.nx, p.nz, p.method, p.precision)])
-    b = capi.Batch(plist)
+    b = capi.Batch(plist, persistent=persistent)
     for i, ph in enumerate(phis):
         b.set_phi(i, ph)
     b.run(3)
@@ -284,7 +288,10 @@ def batched(steps: int, tune: bool = False):
             "xy_paths": {f"{k[0]}x{k[0]}x{k[1]}": PATH_NAMES[v] for k, v in tuned.items()} or "size rule",
             "attempts": r["attempts"], "device_ms": r["device_ms"],
             "what": "config 4: 64 vesicles, grids U{32,48,64,96,128}^3 (seed 4), alpha x U[0.6,0.95], ETD-RK2 "
-                    "per-instance adaptive dt, one CUDA graph per attempt over all size classes, FP32 form; "
+                    "per-instance adaptive dt, FP32 form; "
+                    + ("one persistent kernel per attempt walking a work list of (instance, pass, tile) units"
+                       if persistent else "one CUDA graph per attempt over all size classes, a launch per pass "
+                       "and class") + "; "
                     + ("xy path per size class chosen by cb_autotune" if tune else "xy path by the size rule")}
 
 
@@ -467,7 +474,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--only", choices=["batched", "served"], default=None,
+    ap.add_argument("--only", choices=["batched", "batched_persistent", "served"], default=None,
                     help="run one extra workload alone and print its JSON (for profiling it)")
     ap.add_argument("--tune", action="store_true", help="choose xy paths with cb_autotune (default: size rule)")
     args = ap.parse_args()
@@ -498,8 +505,10 @@ def main():
         if rank == 0:
             import torch
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-            r = batched(min(args.steps, 60), args.tune) if args.only == "batched" else \
-                served(SERVE_TRACE_S, SERVE_MAX_STEPS, args.tune)
+            if args.only == "served":
+                r = served(SERVE_TRACE_S, SERVE_MAX_STEPS, args.tune)
+            else:
+                r = batched(min(args.steps, 60), args.tune, persistent=args.only == "batched_persistent")
             print(json.dumps({"only": args.only, args.only: r}))
         return
     if world > 1:
@@ -511,6 +520,10 @@ def main():
         res["plain_fp64"] = pf
         res["speedup_fp32_over_plain_fp64"] = res["value"] / pf["value"]
         res["batched"] = batched(min(args.steps, 60), args.tune)
+        try:
+            res["batched_persistent"] = batched(min(args.steps, 60), False, persistent=True)
+        except Exception as e:  # reported, not fatal: the default mode above is the batched figure
+            res["batched_persistent"] = {"error": str(e)}
         res["served"] = served(SERVE_TRACE_S, SERVE_MAX_STEPS, args.tune)
         res["ref_cufft"] = ref_cufft(args.steps)
         if "value" in res["ref_cufft"]:

@@ -20,8 +20,8 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libcbstep.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_f32.cu", "kernels_f32_z.cu", "kernels_f64.cu", "kernels_f64_z.cu", "stepper.cu", "pool.cu",
-           "noalloc.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f32_z.cu", "kernels_f64.cu", "kernels_f64_z.cu", "kernels_mega.cu", "stepper.cu",
+           "pool.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

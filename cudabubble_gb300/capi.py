@@ -111,6 +111,7 @@ SIGNATURES = {
     "cb_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
     "cb_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_longlong, _P(C.c_double), _P(C.c_int)]),
     "cb_batch_create": (C.c_int, [_P(cb_params), C.c_int, _P(C.c_void_p)]),
+    "cb_batch_create_ex": (C.c_int, [_P(cb_params), C.c_int, C.c_int, _P(C.c_void_p)]),
     "cb_batch_destroy": (C.c_int, [C.c_void_p]),
     "cb_batch_set_phi": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "cb_batch_get_phi": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
@@ -311,13 +312,19 @@ class Stepper:
         return res
 
 
-class Batch:
-    """Many vesicles of uneven grids advanced together (``cb_batch``)."""
+CB_BATCH_PERSISTENT = 1
 
-    def __init__(self, params_list):
+
+class Batch:
+    """Many vesicles of uneven grids advanced together (``cb_batch``).
+    ``persistent``: one persistent kernel per attempt of every instance
+    (``CB_BATCH_PERSISTENT``) instead of a launch per pass and grid size."""
+
+    def __init__(self, params_list, persistent: bool = False):
         arr = (cb_params * len(params_list))(*params_list)
         h = C.c_void_p()
-        check(lib().cb_batch_create(arr, len(params_list), C.byref(h)))
+        flags = CB_BATCH_PERSISTENT if persistent else 0
+        check(lib().cb_batch_create_ex(arr, len(params_list), flags, C.byref(h)))
         self.h = h
         self.shapes = [(p.nz, p.nx, p.nx) for p in params_list]
 

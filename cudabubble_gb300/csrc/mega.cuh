@@ -1,0 +1,150 @@
+// The persistent batched attempt (FP32 form, ETD-RK2): one launch of two-CTA clusters
+// runs one attempt of every instance of a batched pool by walking the work list of
+// mega.h.  The units run the same pass bodies as the one-pass kernels (z_body,
+// xyc_body, xy_body, prologue_body with PDL = false), on 512-thread CTAs:
+//   z tiles of 32 columns (one CTA each; the one-pass z kernel takes 16 columns on 256
+//   threads), planes from 64^2 on both CTAs of the cluster, smaller planes one per CTA.
+// Each instance keeps its own dt and decision, so its result does not depend on the
+// other instances of the pool; it differs from the per-class graph only in the
+// summation order of its partial sums (tile and thread shapes).
+//
+// Hand-over: rank 0 of a cluster claims the next unit from the shared counter while
+// the current one runs and leaves it in one of two slots of its shared memory; a
+// cluster barrier per unit hands it to rank 1 (which reads it through distributed
+// shared memory), so both CTAs run the same sequence of units and meet the same
+// cluster barriers inside the cluster xy body.
+//
+// Waits: thread 0 of a CTA polls the previous phase's completion counter of the unit's
+// instance with a bounded number of polls.  A wait that runs out counts in err and the
+// unit runs anyway (its results are then not used: the pool reports the attempt as
+// failed), so the control flow of the two CTAs of a cluster never parts.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "mega.h"
+#include "misc_kernels.cuh"
+#include "xy_cluster.cuh"
+#include "xy_kernel.cuh"
+#include "z_kernel.cuh"
+
+namespace cb {
+
+// the grid edges the kernel is built for (each adds a z body and an xy body)
+#ifndef CB_MEGA_SIZES
+#define CB_MEGA_SIZES(X) X(32) X(48) X(64) X(96) X(128)
+#endif
+// polls of a dependency counter before the wait is given up (64-ns sleeps and an L2
+// load each: ~0.1 s, some hundred times a unit's longest legitimate wait)
+#ifndef CB_MEGA_SPIN
+#define CB_MEGA_SPIN (1 << 20)
+#endif
+
+template <int N> __device__ __noinline__ void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm) {
+    ZArgs za = {};
+    za.mode = mode;
+    za.role = mode == Z_ETD2_S1 ? R_WORK : R_CAND;
+    z_body<float, N, kMegaZTX, kMegaThreads, ZG_ETD2, 0, false>(I, tile, za, sm);
+}
+
+template <int N> __device__ __noinline__ void mega_xy(const InstT<float>& I, int plane, int role, unsigned char* sm) {
+    XYArgs xa = {};
+    xa.mode = XY_FUSED;
+    xa.role = role;
+    if constexpr (mega_cluster_xy(N)) xyc_body<float, N, kMegaThreads, 0, false>(I, plane, xa, sm);
+    else xy_body<float, N, kMegaThreads, 2, 0, false>(I, plane, xa, sm);
+}
+
+__device__ __noinline__ void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, unsigned char* head) {
+    ProState* s = reinterpret_cast<ProState*>(head + 16);
+    int* last = reinterpret_cast<int*>(head + 12);
+    prologue_body<float>(I, blk, nblk, accurate, 0, s, last);
+}
+
+static_assert(sizeof(ProState) + 16 <= kMegaHead, "the prologue's shared state fits the head");
+
+__device__ __noinline__ void mega_decide(const InstT<float>& I) { decide_one(I, 0); }
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) mega_kernel(const MegaArgs a) {
+    namespace cg = cooperative_groups;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int tid = threadIdx.x;
+    // head: [0], [1] the hand-over slots (read in rank 0's copy), [2] this CTA's unit
+    unsigned* box = reinterpret_cast<unsigned*>(smem_raw);
+    const unsigned* src = rank == 0 ? box : cl.map_shared_rank(box, 0);
+    unsigned char* sm = smem_raw + kMegaHead;
+    unsigned claimed = 0;  // rank 0, thread 0: the unit of the next round
+    if (rank == 0 && tid == 0) claimed = atomicAdd(a.ticket, 1u);
+    for (int round = 0;; ++round) {
+        if (rank == 0 && tid == 0) box[round & 1] = claimed;
+        // the round's unit is in rank 0's slot; both CTAs are done with the last round
+        cl.sync();
+        if (tid == 0) box[2] = src[round & 1];
+        __syncthreads();
+        const unsigned t = box[2];
+        if (t >= (unsigned)a.ntasks) break;
+        if (rank == 0 && tid == 0) claimed = atomicAdd(a.ticket, 1u);  // under this round's work
+        const MegaTask task = a.tasks[t];
+        const int slot = task.inst * MP_N + task.phase;
+        if (tid == 0 && task.phase != MP_PRO) {
+            const volatile unsigned* d = a.done + slot - 1;
+            const volatile unsigned* failed = a.err;
+            const unsigned need = a.need[slot - 1];
+            int n = 0;
+            // once any wait of the launch has run out, none waits: the attempt is void and
+            // ends without a further bound's delay per unit
+            while (*d < need && *failed == 0u) {
+                if (++n > CB_MEGA_SPIN) {
+                    atomicAdd(a.err, 1u);
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();  // the previous phase's writes before this unit's reads
+        }
+        __syncthreads();
+        const InstT<float>& I = *a.insts[task.inst];
+        const int n = task.size & 0xffff;
+        const int part = 2 * task.unit + rank;
+        switch (task.phase) {
+            case MP_PRO:
+                mega_pro(I, part, (int)a.need[slot], task.size >> 16, smem_raw);
+                break;
+            case MP_Z1:
+            case MP_Z2: {
+                const int mode = task.phase == MP_Z1 ? Z_ETD2_S1 : Z_ETD2_S2;
+                switch (n) {
+#define CASE(N) case N: mega_z<N>(I, part, mode, sm); break;
+                    CB_MEGA_SIZES(CASE)
+#undef CASE
+                    default: break;
+                }
+                break;
+            }
+            default: {  // MP_XYW, MP_XYC
+                const int role = task.phase == MP_XYW ? R_WORK : R_CAND;
+                const int plane = mega_cluster_xy(n) ? task.unit : part;
+                switch (n) {
+#define CASE(N) case N: mega_xy<N>(I, plane, role, sm); break;
+                    CB_MEGA_SIZES(CASE)
+#undef CASE
+                    default: break;
+                }
+                break;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();  // this CTA's writes before its completion count
+            const unsigned prev = atomicAdd(a.done + slot, 1u);
+            if (task.phase == MP_XYC && prev + 1 == a.need[slot]) {
+                __threadfence();  // every CTA of the phase has counted: their sums are final
+                mega_decide(I);
+            }
+        }
+    }
+    cl.sync();  // neither CTA leaves while its partner may read its slots
+}
+
+}  // namespace cb

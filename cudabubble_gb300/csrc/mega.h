@@ -1,0 +1,107 @@
+// Persistent batched attempt (FP32 form, ETD-RK2): the work list and the arguments of
+// the one kernel that runs one attempt of every instance of a batched pool
+// (mega.cuh), shared by the host side (pool.cu) and the device side.
+//
+// An attempt of one instance is five phases, each a set of units:
+//   MP_PRO  prologue and coefficient-table fill      (units of two 512-thread blocks)
+//   MP_Z1   z pass, stage 1                          (units of two 32-column tiles)
+//   MP_XYW  fused xy pass of the work stage           (a plane on both CTAs of a cluster
+//                                                     from 64^2, else two planes)
+//   MP_Z2   z pass, stage 2                          (as MP_Z1)
+//   MP_XYC  fused xy pass of the candidate, then the decision (the CTA that ends the
+//           phase runs it)
+// The work list holds every unit of every instance in phase-major order (largest grids
+// first within a phase).  Persistent two-CTA clusters claim units in list order from
+// one counter, so a unit waits only on units claimed before it and the walk cannot
+// deadlock whatever number of clusters is resident.  A unit waits (bounded) until the
+// counter of its instance's previous phase is complete.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "cb_inst.h"
+
+namespace cb {
+
+enum MegaPhase { MP_PRO = 0, MP_Z1 = 1, MP_XYW = 2, MP_Z2 = 3, MP_XYC = 4, MP_N = 5 };
+
+struct MegaTask {
+    int phase;  // MegaPhase
+    int inst;   // index into MegaArgs::insts
+    int unit;   // CTA rank r of the cluster runs part 2 unit + r (a plane: the unit itself
+                // on the cluster pass)
+    int size;   // grid edge of the phase's transform (nz for z, nx for xy); bit 16: the
+                // class's accurate-coefficient mode
+};
+
+struct MegaArgs {
+    const MegaTask* tasks;
+    const InstT<float>* const* insts;  // table entries of the pool's classes
+    const unsigned* need;              // [inst][MP_N] CTA completions that end each phase
+    unsigned* done;                    // [inst][MP_N] completions of this attempt (zeroed before)
+    unsigned* ticket;                  // next unclaimed unit (zeroed before)
+    unsigned* err;                     // waits that ran out of their bound (0 when healthy)
+    int ntasks;
+    int pad;
+};
+
+constexpr int kMegaThreads = 512;  // threads of every CTA: one plane half, one z tile, ...
+constexpr int kMegaZTX = 32;       // z-tile columns of one CTA (16 threads per column)
+constexpr int kMegaHead = 128;     // dynamic shared-memory bytes before the bodies' region
+constexpr int kMegaProRows = 1024; // coefficient-table entries per prologue unit (two blocks)
+
+// planes of n^2 run on two-CTA clusters (both CTAs of a unit), smaller ones one per CTA
+__host__ __device__ constexpr bool mega_cluster_xy(int n) { return n >= 64; }
+
+// one size class of the pool: instances [first, first + cap) of the instance table
+struct MegaClass {
+    int nx, nz, accurate, cap, first;
+};
+
+// units of phase ph for one instance of class c
+inline int mega_units(const MegaClass& c, int ph) {
+    const int nc = c.nx / 2 + 1;
+    const int kmax = 2 * (c.nx / 2) * (c.nx / 2) + (c.nz / 2) * (c.nz / 2);
+    const int ztiles = (c.nx * nc + kMegaZTX - 1) / kMegaZTX;
+    switch (ph) {
+        case MP_PRO: return std::max(1, (kmax + 1 + kMegaProRows - 1) / kMegaProRows);
+        case MP_Z1:
+        case MP_Z2: return (ztiles + 1) / 2;
+        default: return mega_cluster_xy(c.nx) ? c.nz : (c.nz + 1) / 2;
+    }
+}
+
+// The work list of one attempt (phase-major, larger grids first within a phase) and the
+// CTA completions that end each phase of each instance (need[inst * MP_N + phase]).
+inline void mega_plan(const std::vector<MegaClass>& cls, std::vector<MegaTask>& tasks,
+                      std::vector<unsigned>& need) {
+    int ninst = 0;
+    for (auto& c : cls) ninst = std::max(ninst, c.first + c.cap);
+    need.assign((size_t)ninst * MP_N, 0u);
+    tasks.clear();
+    std::vector<int> order(cls.size());
+    for (size_t i = 0; i < cls.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long long)cls[a].nx * cls[a].nx * cls[a].nz > (long long)cls[b].nx * cls[b].nx * cls[b].nz;
+    });
+    for (int ph = 0; ph < MP_N; ++ph)
+        for (int ci : order) {
+            const MegaClass& c = cls[ci];
+            const int u = mega_units(c, ph);
+            const int size = ((ph == MP_Z1 || ph == MP_Z2) ? c.nz : c.nx) | (c.accurate ? 1 << 16 : 0);
+            for (int k = 0; k < c.cap; ++k) {
+                const int inst = c.first + k;
+                need[(size_t)inst * MP_N + ph] = 2u * (unsigned)u;
+                for (int j = 0; j < u; ++j) tasks.push_back(MegaTask{ph, inst, j, size});
+            }
+        }
+}
+
+bool mega_size_ok(int n);                 // n is a grid edge the kernel is built for
+size_t mega_smem_bytes();                 // dynamic shared memory of one CTA
+int mega_max_clusters();                  // two-CTA clusters resident at once (0: error)
+cudaError_t mega_launch(const MegaArgs& a, int nclusters, cudaStream_t s);
+
+}  // namespace cb

@@ -120,8 +120,8 @@ __device__ inline double lin_coef(const Params& p, int k2) {
     return p.eta * kappa * (D * p.d_ieps3 + p.cx * (double)k2 * p.d_ieps);
 }
 
-// Fills this block's share of table `slot` for time step dt (all blocks of the grid
-// together fill entries 0..kmax).
+// Fills block `blk`'s share of table `slot` for time step dt (blocks 0..nblk-1 of
+// blockDim.x threads together fill entries 0..kmax).
 // L(k) follows Calc.cu:579-606 with c = -cx |k|^2 (kappa = 2, D = 1.5).
 // accurate == 0 evaluates the reference's own closed forms (Calc.cu:446-569);
 // accurate == 1 uses phi-functions, free of the small-|hL| cancellation.
@@ -132,10 +132,11 @@ __device__ inline double lin_coef(const Params& p, int k2) {
 // and its state update is base (+) (em' base + increment) in double-float
 // arithmetic (z_kernel.cuh, State<float>).
 template <class T>
-__device__ inline void fill_table(const InstT<T>& I, const Params& p, int slot, double dt, int accurate) {
+__device__ inline void fill_table(const InstT<T>& I, const Params& p, int slot, double dt, int accurate, int blk,
+                                  int nblk) {
     const double kappa = 2.0, D = 1.5, eps = p.eps, ie = p.d_ieps, ie2 = p.d_ieps2;
     T* tab = I.coef + (size_t)slot * (size_t)(p.kmax + 1) * 8;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx <= p.kmax; idx += gridDim.x * blockDim.x) {
+    for (int idx = blk * blockDim.x + threadIdx.x; idx <= p.kmax; idx += nblk * blockDim.x) {
         const double c = -(double)idx * p.cx;
         const double L = -eps * c * c + kappa * c * ie + D * (c - kappa * ie2) * ie;
         T* out = tab + 8 * (size_t)idx;
@@ -202,24 +203,25 @@ __device__ inline void fill_table(const InstT<T>& I, const Params& p, int slot, 
 // previous kernel left (prologue_state reads only), fills its share of the table when
 // dt is new, and the last block to finish writes the new state: every block has read
 // the old state before it counts itself done, so none sees a half-written one.
+// Block `blk` of the nblk blocks of one instance's prologue (all threads of the CTA);
+// sp and lastp point to the block's shared copies of the new state and of the
+// last-block flag.
 template <class T>
-__global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int accurate, int raw) {
-    CB_PDL_TRIGGER();
-    CB_PDL_WAIT();
-    const InstT<T>& I = insts[blockIdx.y];
+__device__ __forceinline__ void prologue_body(const InstT<T>& I, int blk, int nblk, int accurate, int raw,
+                                              ProState* sp, int* lastp) {
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
-    __shared__ ProState s;
-    __shared__ int last;
+    ProState& s = *sp;
     if (threadIdx.x == 0) s = prologue_state(p, ctrl, raw);
     __syncthreads();
     if (s.skip) return;
-    if (s.fill_slot >= 0) fill_table<T>(I, p, s.fill_slot, s.dt, accurate);
+    if (s.fill_slot >= 0) fill_table<T>(I, p, s.fill_slot, s.dt, accurate, blk, nblk);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned prev = atomicAdd(&ctrl->fill_cnt, 1u);
-        last = prev == gridDim.x - 1;
+        const int last = prev == (unsigned)(nblk - 1);
+        *lastp = last;
         if (last) {
             ctrl->fill_cnt = 0u;
             ctrl->dt = s.dt;
@@ -235,6 +237,14 @@ __global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int acc
         }
     }
 }
+template <class T>
+__global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int accurate, int raw) {
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
+    __shared__ ProState s;
+    __shared__ int last;
+    prologue_body<T>(insts[blockIdx.y], blockIdx.x, gridDim.x, accurate, raw, &s, &last);
+}
 
 // Accept / reject after one attempt (one thread per instance).
 //   adaptive: reject when E_new > E_old, halve dt (belastic.cpp:653-668 and :380-394);
@@ -244,7 +254,7 @@ __global__ void prologue_fill_kernel(const InstT<T>* __restrict__ insts, int acc
 //   raw:      1: accept unconditionally (a single reference step body);
 //             2: accept nothing and keep dt (attempts timed by the autotuner)
 // Exit tests follow belastic.cpp:400-428 (Euler) and :712-740 (ETD).
-// The decision on a copy of the control state (decide_kernel writes it back).
+// The decision on a copy of the control state (decide_one writes it back).
 __device__ inline void decide_update(Ctrl* c, const Params& p, int raw) {
     c->attempts++;
     if (raw == 2) {  // a timing attempt: the state, dt and counters stay, the next attempt is fresh
@@ -332,19 +342,23 @@ __device__ inline void decide_update(Ctrl* c, const Params& p, int raw) {
 // batch of independent loads, the decision runs on the copies, and the state is
 // written back in one batch: a chain of dependent global loads otherwise sets the
 // kernel's length.
-template <class T>
-__global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
-    CB_PDL_TRIGGER();
-    CB_PDL_WAIT();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const InstT<T>& I = insts[i];
+// the decision of one instance on a register copy of its control block
+template <class T> __device__ __forceinline__ void decide_one(const InstT<T>& I, int raw) {
     Ctrl* g = I.ctrl;
     Ctrl c = *g;
     if (c.done) return;
     const Params p = I.p;
     decide_update(&c, p, raw);
     *g = c;
+}
+
+template <class T>
+__global__ void decide_kernel(const InstT<T>* __restrict__ insts, int n, int raw) {
+    CB_PDL_TRIGGER();
+    CB_PDL_WAIT();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    decide_one(insts[i], raw);
 }
 
 // ---------------------------------------------------------- slow path

@@ -17,7 +17,9 @@
 #include <iterator>
 #include <map>
 #include <thread>
+#include <type_traits>
 
+#include "mega.h"
 #include "stepper.cuh"
 
 namespace cb {
@@ -86,6 +88,11 @@ template <class T> class Pool {
         }
         cudaFree(dummy_ctrl);
         cudaFreeHost(h_sum);
+        cudaFree(m_tasks);
+        cudaFree(m_insts);
+        cudaFree(m_need);
+        cudaFree(m_done);
+        cudaFree(m_err);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -162,6 +169,7 @@ template <class T> class Pool {
         int total = 0;
         for (auto& c : cls) total += c.cap;
         CB_CK(cudaMallocHost(&h_sum, sizeof(SlotSummary) * (total > 0 ? total : 1)));
+        if (persistent) return build_mega_graph();
         cudaGraph_t gr = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t r = cudaSuccess;
@@ -183,6 +191,89 @@ template <class T> class Pool {
         cudaError_t ie = cudaGraphInstantiate(&g, gr, 0);
         cudaGraphDestroy(gr);
         CB_CK(ie);
+        return CB_OK;
+    }
+
+    // ---- the persistent batched attempt (mega.h): one kernel per attempt of every
+    // instance instead of a launch per pass and class
+    bool persistent = false;
+    int mega_clusters = 0, mega_tasks = 0;
+
+    int mega_check() const {
+        if (!std::is_same<T, float>::value) return fail(CB_EUNSUPPORTED, "persistent batch: FP32 form only");
+        for (auto& c : cls) {
+            if (c.method != M_ETD2) return fail(CB_EUNSUPPORTED, "persistent batch: ETD-RK2 only");
+            if (c.curv) return fail(CB_EUNSUPPORTED, "persistent batch: no spontaneous curvature");
+            if (!mega_size_ok(c.nx) || !mega_size_ok(c.nz))
+                return fail(CB_EUNSUPPORTED, "persistent batch: grid %dx%dx%d not built into its kernel", c.nx, c.nx,
+                            c.nz);
+            const bool clus = mega_cluster_xy(c.nx);
+            if (c.split == XYP_SPLIT || (clus && c.split == XYP_SINGLE) || (!clus && c.split == XYP_CLUSTER))
+                return fail(CB_EUNSUPPORTED, "persistent batch: xy path %d of %d^2 planes not built into its kernel",
+                            c.split, c.nx);
+        }
+        return CB_OK;
+    }
+
+    // the work list (phase-major, larger grids first), the per-phase completion counts,
+    // and a graph of one attempt: zero the counters, launch the persistent kernel
+    int build_mega_graph() {
+        int rc = mega_check();
+        if (rc) return rc;
+        std::vector<const InstT<float>*> ptrs;
+        std::vector<MegaClass> mc;
+        for (size_t c = 0; c < cls.size(); ++c) {
+            mc.push_back(MegaClass{cls[c].nx, cls[c].nz, cls[c].accurate, cls[c].cap, (int)ptrs.size()});
+            for (int k = 0; k < cls[c].cap; ++k) ptrs.push_back(reinterpret_cast<const InstT<float>*>(cls[c].table + k));
+        }
+        std::vector<MegaTask> tasks;
+        std::vector<unsigned> need;
+        mega_plan(mc, tasks, need);
+        mega_tasks = (int)tasks.size();
+        const int maxc = mega_max_clusters();
+        if (maxc <= 0) return fail(CB_ECUDA, "persistent batch: no resident cluster of its kernel");
+        mega_clusters = std::min(maxc, std::max(1, mega_tasks));
+        CB_CK(cudaMalloc(&m_tasks, sizeof(MegaTask) * tasks.size()));
+        CB_CK(cudaMalloc(&m_insts, sizeof(void*) * ptrs.size()));
+        CB_CK(cudaMalloc(&m_need, sizeof(unsigned) * need.size()));
+        CB_CK(cudaMalloc(&m_done, sizeof(unsigned) * (need.size() + 1)));  // + the unit counter
+        CB_CK(cudaMalloc(&m_err, sizeof(unsigned)));
+        CB_CK(cudaMemcpy(m_tasks, tasks.data(), sizeof(MegaTask) * tasks.size(), cudaMemcpyHostToDevice));
+        CB_CK(cudaMemcpy(m_insts, ptrs.data(), sizeof(void*) * ptrs.size(), cudaMemcpyHostToDevice));
+        CB_CK(cudaMemcpy(m_need, need.data(), sizeof(unsigned) * need.size(), cudaMemcpyHostToDevice));
+        CB_CK(cudaMemset(m_err, 0, sizeof(unsigned)));
+        MegaArgs a;
+        memset(&a, 0, sizeof a);
+        a.tasks = m_tasks;
+        a.insts = m_insts;
+        a.need = m_need;
+        a.done = m_done;
+        a.ticket = m_done + need.size();
+        a.err = m_err;
+        a.ntasks = mega_tasks;
+        cudaGraph_t gr = nullptr;
+        CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t r = cudaMemsetAsync(m_done, 0, sizeof(unsigned) * (need.size() + 1), st);
+        if (r == cudaSuccess) r = mega_launch(a, mega_clusters, st);
+        cudaError_t e = cudaStreamEndCapture(st, &gr);
+        if (r != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return fail(CB_ECUDA, "persistent batch capture: %s", cudaGetErrorString(r));
+        }
+        CB_CK(e);
+        cudaError_t ie = cudaGraphInstantiate(&g, gr, 0);
+        cudaGraphDestroy(gr);
+        CB_CK(ie);
+        return CB_OK;
+    }
+
+    // waits of the persistent kernel that ran out since the last call (synchronises)
+    int mega_failures(unsigned* n) {
+        *n = 0;
+        if (!persistent) return CB_OK;
+        CB_CK(cudaMemcpyAsync(n, m_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CB_CK(cudaStreamSynchronize(st));
+        if (*n) CB_CK(cudaMemset(m_err, 0, sizeof(unsigned)));
         return CB_OK;
     }
 
@@ -222,6 +313,11 @@ template <class T> class Pool {
     Ctrl* dummy_ctrl = nullptr;
     InstT<T> dummy{};
     SlotSummary* h_sum = nullptr;
+    MegaTask* m_tasks = nullptr;
+    const InstT<float>** m_insts = nullptr;
+    unsigned* m_need = nullptr;
+    unsigned* m_done = nullptr;
+    unsigned* m_err = nullptr;
 };
 
 // ---------------------------------------------------------------- batch
@@ -241,10 +337,11 @@ template <class T> class Batch final : public BatchBase {
         items.clear();
         cudaFree(flush_buf);
     }
-    int init(const cb_params* ps, int n) {
+    int init(const cb_params* ps, int n, bool persistent = false) {
         pool.reset(new Pool<T>());
         int rc = pool->init();
         if (rc) return rc;
+        pool->persistent = persistent;
         for (int i = 0; i < n; ++i) {
             std::unique_ptr<Stepper<T>> s(new Stepper<T>());
             rc = s->init(ps[i]);
@@ -322,6 +419,10 @@ template <class T> class Batch final : public BatchBase {
             }
             int rc = pool->poll(sum);
             if (rc) return rc;
+            unsigned lost = 0;
+            rc = pool->mega_failures(&lost);
+            if (rc) return rc;
+            if (lost) return fail(CB_ETIMEOUT, "persistent batch: %u dependency waits ran out", lost);
             all = true;
             for (auto& w : where)
                 if (!sum[pool->slot_index(w.first, w.second)].done) { all = false; break; }
@@ -791,8 +892,12 @@ struct cb_batch {
 
 extern "C" {
 
-int cb_batch_create(const cb_params* ps, int n, cb_batch** out) {
+int cb_batch_create(const cb_params* ps, int n, cb_batch** out) { return cb_batch_create_ex(ps, n, 0, out); }
+
+int cb_batch_create_ex(const cb_params* ps, int n, int flags, cb_batch** out) {
     if (!ps || n <= 0 || !out) return cb::fail(CB_EINVAL, "bad batch arguments");
+    if (flags & ~CB_BATCH_PERSISTENT) return cb::fail(CB_EINVAL, "unknown batch flags %d", flags);
+    const bool persistent = (flags & CB_BATCH_PERSISTENT) != 0;
     *out = nullptr;
     for (int i = 1; i < n; ++i)
         if (ps[i].precision != ps[0].precision) return cb::fail(CB_EINVAL, "a batch holds one precision");
@@ -801,11 +906,11 @@ int cb_batch_create(const cb_params* ps, int n, cb_batch** out) {
     if (ps[0].precision == CB_FP32) {
         auto* p = new cb::Batch<float>();
         b->impl.reset(p);
-        rc = p->init(ps, n);
+        rc = p->init(ps, n, persistent);
     } else {
         auto* p = new cb::Batch<double>();
         b->impl.reset(p);
-        rc = p->init(ps, n);
+        rc = p->init(ps, n, persistent);
     }
     if (rc) return rc;
     *out = b.release();

@@ -39,23 +39,22 @@ template <class T, int NX, int NQ = 0> constexpr size_t xyc_smem_bytes() {
     return sizeof(cplx<T>) * ((size_t)Q::SZ + Q::SQ + ntw * (Q::M + NX + NX)) + (32 * 4 + 2) * sizeof(double);
 }
 
-template <class T, int NX, int NT, int NQ = 0>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
-    xyc_fused_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
+// Plane z of instance I on this CTA's two-CTA cluster, all NT threads of both CTAs: the
+// body of xyc_fused_kernel (one plane per cluster, PDL = true: programmatic launch) and of
+// the persistent batched kernel (mega.cuh, PDL = false).
+template <class T, int NX, int NT, int NQ = 0, bool PDL = true>
+__device__ __forceinline__ void xyc_body(const InstT<T>& I, const int z, const XYArgs a, unsigned char* smem_raw) {
     namespace cg = cooperative_groups;
     using C = cplx<T>;
     using Q = XYC<NX, NQ>;
     constexpr int M = Q::M, NY = Q::NY, NC = Q::NC, MH = Q::MH, NH = Q::NH, PY = Q::PY, PX = Q::PX;
     constexpr int QX = Q::QX, QY = Q::QY;
     constexpr int ntw = sizeof(T) == 4 ? 2 : 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    CB_PDL_TRIGGER();
+    if constexpr (PDL) CB_PDL_TRIGGER();
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
-    const InstT<T>& I = insts[blockIdx.y];
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
-    const int z = blockIdx.x >> 1;
     const int tid = threadIdx.x;
     const void *p00 = I.P[0][0], *p01 = I.P[0][1], *p10 = I.P[1][0], *p11 = I.P[1][1], *p20 = I.P[2][0],
                *p21 = I.P[2][1];
@@ -82,7 +81,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
     }
     // the twiddles (written by no kernel) are loaded; the control state and the
     // partials come from the previous kernel
-    CB_PDL_WAIT();
+    if constexpr (PDL) CB_PDL_WAIT();
     // the control fields and this pass's candidate partial sets in one batch of
     // independent loads (the state-selected pointers are chosen in registers)
     const int c_done = ctrl->done, c_part = ctrl->part_state, c_u = ctrl->u_state;
@@ -342,6 +341,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
             outB[ky * NC + c] = zh;
         }
     }
+}
+
+template <class T, int NX, int NT, int NQ = 0>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT)
+    xyc_fused_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    xyc_body<T, NX, NT, NQ, true>(insts[blockIdx.y], blockIdx.x >> 1, a, smem_raw);
 }
 
 }  // namespace cb

@@ -110,19 +110,20 @@ __device__ __forceinline__ void nl_outputs(const InstT<T>& I, const Ctrl* c, int
 // NF = fields per plane: 2 for XY_REDUCE_FULL / XY_NONLIN / XY_FUSED, 1 otherwise.
 // NQ = 1: the FP32 fused pass with spontaneous curvature, whose third output field q lives
 // in a region of its own, [NY][M + 1] after the plane (pointwise.cuh, fused_point_u2)
-template <class T, int NX, int NT, int NF, int NQ = 0>
-__global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
+//
+// Plane z of instance I on this CTA, all NT threads: the body of xy_kernel (one plane per
+// CTA, PDL = true: programmatic launch) and of the persistent batched kernel (mega.cuh,
+// PDL = false).
+template <class T, int NX, int NT, int NF, int NQ = 0, bool PDL = true>
+__device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XYArgs a, unsigned char* smem_raw) {
     using C = cplx<T>;
     constexpr int M = NX / 2, NY = NX, NC = M + 1;
     constexpr int nf = NF;
     constexpr int pitch = nf * M + 1;
     constexpr int QX = M + 1, SQ = NQ ? NY * QX : 0;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    CB_PDL_TRIGGER();
-    const InstT<T>& I = insts[blockIdx.y];
+    if constexpr (PDL) CB_PDL_TRIGGER();
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
-    const int z = blockIdx.x;
     const int tid = threadIdx.x;
     if (z >= p.nz) return;
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     }
     // the twiddles (written by no kernel) are loaded; what follows reads the previous
     // kernel's results
-    CB_PDL_WAIT();
+    if constexpr (PDL) CB_PDL_WAIT();
     // the control fields in one batch of independent loads, so the CTA does not wait on a
     // chain of dependent loads before its data moves
     const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_part = ctrl->part_state, c_u = ctrl->u_state;
@@ -484,6 +485,12 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
             }
         }
     }
+}
+
+template <class T, int NX, int NT, int NF, int NQ = 0>
+__global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ insts, XYArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    xy_body<T, NX, NT, NF, NQ, true>(insts[blockIdx.y], blockIdx.x, a, smem_raw);
 }
 
 template <class T, int NX> constexpr size_t xy_smem_bytes(int nf, int nq = 0) {

@@ -130,21 +130,25 @@ __host__ __device__ constexpr int zgroup_of(int mode) {
          : mode == Z_EULER ? ZG_EULER : ZG_PLAIN;
 }
 
+// The pass over one column tile `tile` of instance I, run by all NT threads of the CTA
+// on its dynamic shared memory: the body of z_kernel (one tile per CTA, PDL = true:
+// programmatic launch, waiting for the previous kernel after the twiddle load) and of
+// the persistent batched kernel (mega.cuh, PDL = false: its own dependency counters).
+//
 // NQ = 1 (FP32 stage groups with spontaneous curvature): the stage's third partial q is
 // transformed with A and B and takes B's multiplier, N-hat = (A-hat + beta cx kz^2 (B-hat +
 // q-hat)) / N, while f-hat keeps being rebuilt from B-hat alone
-template <class T, int NZ, int TX, int NT, int MG, int NQ = 0>
-__global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+template <class T, int NZ, int TX, int NT, int MG, int NQ = 0, bool PDL = true>
+__device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const ZArgs a,
+                                       unsigned char* smem_raw) {
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    CB_PDL_TRIGGER();
-    const InstT<T>& I = insts[blockIdx.y];
+    if constexpr (PDL) CB_PDL_TRIGGER();
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
     const int nc = p.nc, ny = p.ny, nx = p.nx;
     const int Mc = ny * nc;
-    const int m0 = blockIdx.x * TX;
+    const int m0 = tile * TX;
     const int tid = threadIdx.x;
     if (m0 >= Mc) return;
     const void* g_a[2] = {I.G[0][0], I.G[1][0]};
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     for (int i = tid; i < ntw * NZ; i += NT) tw[i] = reinterpret_cast<const C*>(I.twz)[i];
     // the twiddles (written by no kernel) are loaded; what follows reads the previous
     // kernel's results
-    CB_PDL_WAIT();
+    if constexpr (PDL) CB_PDL_WAIT();
     // the control fields in one batch of independent loads (the state-selected pointer
     // is chosen in registers), so the CTA does not wait on a chain of dependent loads
     const int c_done = ctrl->done, c_fresh = ctrl->fresh, c_ab = ctrl->ab_state;
@@ -590,8 +594,8 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     double* part = I.part_z;
     int* last = reinterpret_cast<int*>(red + 64);
     if (tid == 0) {
-        part[2 * blockIdx.x + 0] = v[0];
-        part[2 * blockIdx.x + 1] = v[1];
+        part[2 * tile + 0] = v[0];
+        part[2 * tile + 1] = v[1];
         __threadfence();
         const unsigned prev = atomicAdd(&ctrl->cnt_z[a.role], 1u);
         *last = prev == (unsigned)(ntiles - 1);
@@ -607,6 +611,12 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
             ctrl->cnt_z[a.role] = 0u;
         }
     }
+}
+
+template <class T, int NZ, int TX, int NT, int MG, int NQ = 0>
+__global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const InstT<T>* __restrict__ insts, ZArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    z_body<T, NZ, TX, NT, MG, NQ, true>(insts[blockIdx.y], blockIdx.x, a, smem_raw);
 }
 
 template <class T, int NZ, int TX, int NQ = 0> constexpr size_t z_smem_bytes() {

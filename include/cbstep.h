@@ -223,6 +223,16 @@ int cb_profile_kernels(cb_handle* h, int nattempts, long long flush_bytes, doubl
  * accept/reject state and exit test.  All instances share one precision. */
 typedef struct cb_batch cb_batch;
 int cb_batch_create(const cb_params* params, int n, cb_batch** out);
+/* flags = CB_BATCH_PERSISTENT: one persistent kernel runs each attempt of every
+ * instance, walking a device work list of (instance, pass, tile or plane) units with
+ * per-instance dependency counters, instead of one launch per pass and grid size.
+ * FP32 form, ETD-RK2, grids of 32, 48, 64, 96 or 128 per edge, no spontaneous
+ * curvature, the default xy path; otherwise CB_EUNSUPPORTED.  Each instance's
+ * decisions are its own as in the default mode; its sums differ from the default
+ * mode's only in summation order (the kernel's z tiles are 32 columns on 512 threads).
+ * A dependency wait that runs out of its bound makes cb_batch_run return CB_ETIMEOUT. */
+#define CB_BATCH_PERSISTENT 1
+int cb_batch_create_ex(const cb_params* params, int n, int flags, cb_batch** out);
 int cb_batch_destroy(cb_batch* b);
 int cb_batch_set_phi(cb_batch* b, int i, const double* phi, int on_device);
 int cb_batch_get_phi(cb_batch* b, int i, double* phi, int on_device);

@@ -13,11 +13,13 @@
 #include <cmath>
 #include <condition_variable>
 #include <mutex>
+#include <thread>
 
 #define __device__
 #define __host__
 #define __global__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 #define __launch_bounds__(...)
 #define __cluster_dims__(...)
 #define __align__(n) alignas(n)
@@ -115,3 +117,5 @@ inline float2 __fmul2_rn(float2 a, float2 b) { return {a.x * b.x, a.y * b.y}; }
 inline float2 __ffma2_rn(float2 a, float2 b, float2 c) { return {fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)}; }
 
 typedef int cudaError_t;
+typedef struct emu_stream_* cudaStream_t;  // declarations only (the kernel drivers launch through emu::launch)
+inline void __nanosleep(unsigned) { std::this_thread::yield(); }

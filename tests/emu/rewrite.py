@@ -55,7 +55,7 @@ def rewrite_launches(text):
         args = text[e + 4:m]
         smem = cfg[2] if len(cfg) > 2 else "0"
         strm = cfg[3] if len(cfg) > 3 else "0"
-        clus = 2 if "xyc_fused_kernel" in name else 1  # __cluster_dims__(2, 1, 1)
+        clus = 2 if ("xyc_fused_kernel" in name or "mega_kernel" in name) else 1  # __cluster_dims__(2, 1, 1)
         out += (text[i:k + 1] + f"\n    ::emu::launch_kernel(dim3({cfg[0]}), dim3({cfg[1]}), (size_t)({smem}), "
                 f"(cudaStream_t)({strm}), (const void*)(&{name}), {clus}, [=]() {{ {name}({args}); }})")
         i = m + 1
@@ -86,7 +86,7 @@ def rewrite_launch_k(text):
             m += 1
         parts = _split_top(text[j + 9:m])
         name, grid, block, smem, strm, args = parts[0], parts[1], parts[2], parts[3], parts[4], parts[5:]
-        clus = 2 if "xyc_fused_kernel" in name else 1
+        clus = 2 if ("xyc_fused_kernel" in name or "mega_kernel" in name) else 1
         out += (text[i:j] + f"::emu::launch_kernel({grid}, {block}, (size_t)({smem}), (cudaStream_t)({strm}), "
                 f"(const void*)(&{name}), {clus}, [=]() {{ {name}({', '.join(args)}); }})")
         i = m + 1

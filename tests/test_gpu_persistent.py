@@ -1,0 +1,77 @@
+"""The persistent batched attempt (CB_BATCH_PERSISTENT) on the GPU, through the C ABI.
+
+One kernel walks the work list of every instance's attempt.  Each instance keeps its
+own dt and decisions, so against the per-class graph of the default mode the same
+instance takes the same accepted and rejected attempts; its sums differ only in
+summation order (32-column z tiles on 512 threads, 512-thread plane passes), so the
+energies agree to round-off.  Within the persistent mode an instance's trajectory is
+bitwise the same alone and in any mix.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MIX = [(32, 3), (48, 4), (64, 5), (96, 6), (32, 7), (64, 8), (128, 9)]
+
+
+def _params(capi, n, **kw):
+    base = dict(nx=n, ny=n, nz=n, epssize=150, method=capi.CB_ETD2, precision=capi.CB_FP32, time_step=1e-6,
+                fixed_time_step=0.0, M1=1e4, M2=1e4)
+    base.update(kw)
+    return capi.default_params(**base)
+
+
+def _batch(capi, shapes, mix, persistent, steps):
+    plist = [_params(capi, n) for n, _ in mix]
+    phis = [shapes.seeded_ellipsoid(n, n, shapes.eps_rule(150, n), seed) for n, seed in mix]
+    b = capi.Batch(plist, persistent=persistent)
+    for i, phi in enumerate(phis):
+        b.set_phi(i, phi)
+    r = b.run(steps)
+    return b, r
+
+
+def test_persistent_matches_the_per_class_graph(cblib):
+    from cudabubble_gb300 import capi, shapes
+    g, rg = _batch(capi, shapes, MIX, False, 15)
+    m, rm = _batch(capi, shapes, MIX, True, 15)
+    assert rg["steps"] == rm["steps"] == 15 * len(MIX)
+    assert rm["attempts"] == rg["attempts"]
+    for i, (n, _) in enumerate(MIX):
+        sg, sm = g.scalars(i), m.scalars(i)
+        assert (sm["steps"], sm["rejects"], sm["dt"]) == (sg["steps"], sg["rejects"], sg["dt"]), (n, sg, sm)
+        rel = abs(sm["E"] - sg["E"]) / abs(sg["E"])
+        assert rel < 1e-9, (n, rel)
+        assert sm["V"] == pytest.approx(sg["V"], rel=1e-11)
+        assert sm["S"] == pytest.approx(sg["S"], rel=1e-9)
+        d = np.abs(m.get_phi(i) - g.get_phi(i)).max()
+        assert d < 1e-7, (n, d)
+    # a second run continues every instance from where it stopped
+    m.run(3)
+    assert all(m.scalars(i)["steps"] == 18 for i in range(len(MIX)))
+    g.close()
+    m.close()
+
+
+def test_persistent_same_alone_and_in_mix(cblib):
+    """The 64^3 instance (seed 5) alone and among six others: the same bits."""
+    from cudabubble_gb300 import capi, shapes
+    a, _ = _batch(capi, shapes, [(64, 5)], True, 12)
+    m, _ = _batch(capi, shapes, MIX, True, 12)
+    assert np.array_equal(a.get_phi(0), m.get_phi(2))
+    sa, sm = a.scalars(0), m.scalars(2)
+    assert (sa["steps"], sa["rejects"], sa["dt"], sa["E"]) == (sm["steps"], sm["rejects"], sm["dt"], sm["E"])
+    a.close()
+    m.close()
+
+
+@pytest.mark.parametrize("what", ["fp64", "etd4", "n192", "curvature", "split"])
+def test_persistent_refuses_what_it_is_not_built_for(cblib, what):
+    from cudabubble_gb300 import capi
+    kw = {"fp64": dict(precision=capi.CB_FP64), "etd4": dict(method=capi.CB_ETD4), "n192": dict(nx=192, ny=192, nz=32),
+          "curvature": dict(spont_c=0.5), "split": dict(xy_split=capi.XYP_SPLIT)}[what]
+    p = _params(capi, 32, **kw)
+    with pytest.raises(capi.CBError) as ei:
+        capi.Batch([p, _params(capi, 32)] if what != "fp64" else [p], persistent=True)
+    assert ei.value.code == capi.CB_EUNSUPPORTED

@@ -45,6 +45,41 @@ def harness(tmp_path_factory):
     return str(exe)
 
 
+@pytest.fixture(scope="module")
+def mega_harness(tmp_path_factory):
+    """tests/emu/mega_attempt.cpp: one attempt of a three-instance pool through the
+    persistent batched kernel against the one-pass kernels of the same shapes."""
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("emu_mega")
+    src = d / "src"
+    spec = importlib.util.spec_from_file_location("emu_rewrite", os.path.join(EMU, "rewrite.py"))
+    rw = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(rw)
+    rw.copy_sources(CSRC, str(src))
+    exe = d / "mega_attempt"
+    cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer", "-ffp-contract=off",
+           "-I", os.path.join(EMU, "fake"), "-I", str(src), "-I", os.path.join(ROOT, "include"),
+           os.path.join(EMU, "mega_attempt.cpp"), "-o", str(exe), "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr and "cannot find" in r.stderr:
+        pytest.skip("AddressSanitizer runtime not available")
+    assert r.returncode == 0, r.stderr[-4000:]
+    return str(exe)
+
+
+def test_persistent_kernel_same_as_one_pass_kernels(mega_harness):
+    """Work list, unit hand-over between the CTAs of a cluster, dependency counters and the
+    decision by the CTA that ends an instance's last phase: every buffer and control field
+    of the three instances bitwise as the one-pass kernels leave them, all phase counters
+    complete, no wait run out, every index in bounds."""
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1")
+    r = subprocess.run([mega_harness], capture_output=True, text=True, env=env, timeout=3000)
+    assert "AddressSanitizer" not in r.stderr, r.stderr[-6000:]
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert r.stdout.strip().endswith("SAME"), r.stdout[-3000:]
+
+
 METHODS = {"euler": 0, "etd2": 1, "etd4": 2}
 
 
