@@ -114,22 +114,30 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
             case MP_Z1:
             case MP_Z2: {
                 const int mode = task.phase == MP_Z1 ? Z_ETD2_S1 : Z_ETD2_S2;
-                switch (n) {
-#define CASE(N) case N: mega_z<N>(I, part, mode, sm); break;
-                    CB_MEGA_SIZES(CASE)
+                for (int j = 0; j < kMegaZPer; ++j) {
+                    if (j) __syncthreads();  // the last tile's reads of shared memory are done
+                    const int tile = part * kMegaZPer + j;
+                    switch (n) {
+#define CASE(N) case N: mega_z<N>(I, tile, mode, sm); break;
+                        CB_MEGA_SIZES(CASE)
 #undef CASE
-                    default: break;
+                        default: break;
+                    }
                 }
                 break;
             }
             default: {  // MP_XYW, MP_XYC
                 const int role = task.phase == MP_XYW ? R_WORK : R_CAND;
-                const int plane = mega_cluster_xy(n) ? task.unit : part;
-                switch (n) {
+                const int per = mega_cluster_xy(n) ? 1 : kMegaXYPer;
+                for (int j = 0; j < per; ++j) {
+                    if (j) __syncthreads();  // the last plane's reads of shared memory are done
+                    const int plane = mega_cluster_xy(n) ? task.unit : part * kMegaXYPer + j;
+                    switch (n) {
 #define CASE(N) case N: mega_xy<N>(I, plane, role, sm); break;
-                    CB_MEGA_SIZES(CASE)
+                        CB_MEGA_SIZES(CASE)
 #undef CASE
-                    default: break;
+                        default: break;
+                    }
                 }
                 break;
             }

@@ -31,7 +31,8 @@ struct MegaTask {
     int phase;  // MegaPhase
     int inst;   // index into MegaArgs::insts
     int unit;   // CTA rank r of the cluster runs part 2 unit + r (a plane: the unit itself
-                // on the cluster pass)
+                // on the cluster pass), i.e. z tiles or one-CTA planes k PER + j, j < PER,
+                // of k = 2 unit + r
     int size;   // grid edge of the phase's transform (nz for z, nx for xy); bit 16: the
                 // class's accurate-coefficient mode
 };
@@ -46,6 +47,16 @@ struct MegaArgs {
     int ntasks;
     int pad;
 };
+
+// z tiles, and planes of the one-CTA plane pass, that one CTA runs in one unit (build-time
+// schedule knobs)
+#ifndef CB_MEGA_ZPER
+#define CB_MEGA_ZPER 1
+#endif
+#ifndef CB_MEGA_XYPER
+#define CB_MEGA_XYPER 1
+#endif
+constexpr int kMegaZPer = CB_MEGA_ZPER, kMegaXYPer = CB_MEGA_XYPER;
 
 constexpr int kMegaThreads = 512;  // threads of every CTA: one plane half, one z tile, ...
 constexpr int kMegaZTX = 32;       // z-tile columns of one CTA (16 threads per column)
@@ -68,8 +79,8 @@ inline int mega_units(const MegaClass& c, int ph) {
     switch (ph) {
         case MP_PRO: return std::max(1, (kmax + 1 + kMegaProRows - 1) / kMegaProRows);
         case MP_Z1:
-        case MP_Z2: return (ztiles + 1) / 2;
-        default: return mega_cluster_xy(c.nx) ? c.nz : (c.nz + 1) / 2;
+        case MP_Z2: return (ztiles + 2 * kMegaZPer - 1) / (2 * kMegaZPer);
+        default: return mega_cluster_xy(c.nx) ? c.nz : (c.nz + 2 * kMegaXYPer - 1) / (2 * kMegaXYPer);
     }
 }
 
