@@ -34,6 +34,17 @@ namespace cb {
 #define CB_PDL_WAIT() ((void)0)
 #endif
 
+// Release / acquire fence at GPU scope for the counters the kernels sync through (the
+// last CTA of a pass, the persistent batch's phase counters): fence.acq_rel orders this
+// thread's (and, through the CTA barrier before it, its block's) writes before the
+// counter update that follows, and the counter read before the reads that follow.  A
+// build with -DCB_FENCE_SC uses __threadfence (fence.sc.gpu) instead.
+#if defined(__CUDA_ARCH__) && !defined(CB_FENCE_SC)
+#define CB_FENCE() asm volatile("fence.acq_rel.gpu;" ::: "memory")
+#else
+#define CB_FENCE() __threadfence()
+#endif
+
 // ---------------------------------------------------------------- complex
 template <class T> struct CT;
 template <> struct CT<float> { using type = float2; };

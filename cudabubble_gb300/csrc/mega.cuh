@@ -101,7 +101,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
                 }
                 __nanosleep(64);
             }
-            __threadfence();  // the previous phase's writes before this unit's reads
+            CB_FENCE();  // the previous phase's writes before this unit's reads
         }
         __syncthreads();
         const InstT<float>& I = *a.insts[task.inst];
@@ -144,10 +144,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
         }
         __syncthreads();
         if (tid == 0) {
-            __threadfence();  // this CTA's writes before its completion count
+            CB_FENCE();  // this CTA's writes before its completion count
             const unsigned prev = atomicAdd(a.done + slot, 1u);
             if (task.phase == MP_XYC && prev + 1 == a.need[slot]) {
-                __threadfence();  // every CTA of the phase has counted: their sums are final
+                CB_FENCE();  // every CTA of the phase has counted: their sums are final
                 mega_decide(I);
             }
         }

@@ -218,7 +218,7 @@ __device__ __forceinline__ void prologue_body(const InstT<T>& I, int blk, int nb
     if (s.fill_slot >= 0) fill_table<T>(I, p, s.fill_slot, s.dt, accurate, blk, nblk);
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
+        CB_FENCE();
         const unsigned prev = atomicAdd(&ctrl->fill_cnt, 1u);
         const int last = prev == (unsigned)(nblk - 1);
         *lastp = last;

@@ -73,13 +73,13 @@ __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Par
             part[4 * slot + 0] = 0.0;
             part[4 * slot + 3] = 0.0;
         }
-        __threadfence();
+        CB_FENCE();
         const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[role], 1u);
         *last = done_blocks == (unsigned)(nslots - 1);
     }
     __syncthreads();
     if (*last) {  // the last CTA of this instance finalises, with all its threads
-        __threadfence();
+        CB_FENCE();
         double sums[4];
         block_sum_parts<4>(part, nslots, sums, red);
         if (threadIdx.x == 0) {

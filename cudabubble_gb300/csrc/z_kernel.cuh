@@ -596,13 +596,13 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
     if (tid == 0) {
         part[2 * tile + 0] = v[0];
         part[2 * tile + 1] = v[1];
-        __threadfence();
+        CB_FENCE();
         const unsigned prev = atomicAdd(&ctrl->cnt_z[a.role], 1u);
         *last = prev == (unsigned)(ntiles - 1);
     }
     __syncthreads();
     if (*last) {  // the last CTA of this instance finalises, with all its threads
-        __threadfence();
+        CB_FENCE();
         double sums[2];
         block_sum_parts<2>(part, ntiles, sums, red);
         if (tid == 0) {
