@@ -56,6 +56,29 @@ def test_persistent_matches_the_per_class_graph(cblib):
     m.close()
 
 
+@pytest.mark.parametrize("kw", [dict(fixed_time_step=2e-6, accurate_coefficients=1),
+                                dict(fixed_time_step=2e-6, M1=0.0, M2=0.0)],
+                         ids=["fixed-dt-corrected-accurate", "fixed-dt-no-penalty"])
+def test_persistent_fixed_dt_loops(cblib, kw):
+    """The fixed-dt loops (with the alpha/beta correction's redo of a step, and without
+    penalties) through the persistent kernel against the per-class graph."""
+    from cudabubble_gb300 import capi, shapes
+    mix = [(32, 11), (64, 12), (48, 13)]
+    out = []
+    for persistent in (False, True):
+        plist = [_params(capi, n, **kw) for n, _ in mix]
+        b = capi.Batch(plist, persistent=persistent)
+        for i, (n, seed) in enumerate(mix):
+            b.set_phi(i, shapes.seeded_ellipsoid(n, n, shapes.eps_rule(150, n), seed))
+        b.run(8)
+        out.append([b.scalars(i) for i in range(len(mix))])
+        b.close()
+    for (n, _), sg, sm in zip(mix, *out):
+        assert (sm["steps"], sm["rejects"], sm["attempts"], sm["dt"]) == (sg["steps"], sg["rejects"], sg["attempts"],
+                                                                          sg["dt"]), n
+        assert abs(sm["E"] - sg["E"]) <= 1e-7 * abs(sg["E"]), (n, sm["E"], sg["E"])
+
+
 def test_persistent_same_alone_and_in_mix(cblib):
     """The 64^3 instance (seed 5) alone and among six others: the same bits."""
     from cudabubble_gb300 import capi, shapes
