@@ -161,15 +161,38 @@ def cpu_reference_run(nsteps: int, warmup: int, threads: int = 0):
     return dict(seconds=dt, steps=sc["steps"], why=why, threads=cs.threads, E=sc["E"])
 
 
+def cpu_c1_run(nsteps: int, threads: int):
+    """Config 1 on the host cores: 64^3, axes (1.6, 1.6, 0.8), eps = 2h, forward Euler at
+    fixed dt 1e-7, M1 = M2 = 1e4 (oracle/cstep.c, FP64)."""
+    from oracle.cbuild import CStep
+    from cudabubble_gb300 import shapes
+    n = 64
+    eps = shapes.eps_rule(200, n)
+    p0 = shapes.ellipsoid(n, n, eps, (1.6, 1.6, 0.8))
+    cs = CStep(n, n, eps, threads=threads)
+    cs.set_phi(p0)
+    t0 = time.perf_counter()
+    cs.run("euler", nsteps, 1e-7, 1e-7)
+    dt = time.perf_counter() - t0
+    sc = cs.scalars()
+    cs.close()
+    return dict(seconds=dt, steps=sc["steps"], threads=cs.threads)
+
+
 def cpu_baseline():
-    """Bounded samples of the workload on the host cores (oracle/cstep.c, the plain FP64
-    C port of the reference step): steps 1..20 with OpenMP on every host thread, median
-    of 5 runs, and steps 1..4 on one thread, median of 3 runs (~30 s of CPU work in all)."""
-    def median_run(nsteps, runs, threads):
-        rs = sorted((cpu_reference_run(nsteps, 0, threads) for _ in range(runs)), key=lambda r: r["seconds"])
+    """Bounded samples on the host cores (oracle/cstep.c, the plain FP64 C port of the
+    reference step).  The workload (config 2): steps 1..20 (the GPU arm's K) with OpenMP on
+    every host thread, median of 5 runs, and steps 1..4 on one thread, median of 3.
+    Config 1 (64^3 Euler): 100 steps with OpenMP, median of 5, and 20 steps on one thread,
+    median of 3.  About 35 s of CPU work in all."""
+    def median(fn, nsteps, runs, threads):
+        rs = sorted((fn(nsteps, threads) for _ in range(runs)), key=lambda r: r["seconds"])
         return rs[len(rs) // 2]
-    omp = median_run(20, 5, os.cpu_count() or 0)
-    one = median_run(4, 3, 1)
+    allt = os.cpu_count() or 0
+    omp = median(lambda k, t: cpu_reference_run(k, 0, t), 20, 5, allt)
+    one = median(lambda k, t: cpu_reference_run(k, 0, t), 4, 3, 1)
+    c1 = median(cpu_c1_run, 100, 5, allt)
+    c1s = median(cpu_c1_run, 20, 3, 1)
     v = N_GRID ** 3 * omp["steps"] / omp["seconds"]
     v1 = N_GRID ** 3 * one["steps"] / one["seconds"]
     return {"value": v, "unit": UNIT, "cores": omp["threads"], "kind": "port",
@@ -177,7 +200,14 @@ def cpu_baseline():
                       f"{omp['threads']} threads), median of 5 runs, {omp['seconds']:.2f} s each",
             "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
                               "sample": f"steps 1..{one['steps']}, one thread, median of 3 runs, "
-                                        f"{one['seconds']:.2f} s each"}}
+                                        f"{one['seconds']:.2f} s each"},
+            "config1": {"value": 64 ** 3 * c1["steps"] / c1["seconds"], "unit": UNIT, "cores": c1["threads"],
+                        "sample": f"config 1 (64^3, Euler, fixed dt 1e-7), {c1['steps']} steps, OpenMP on "
+                                  f"{c1['threads']} threads, median of 5 runs, {c1['seconds']:.2f} s each",
+                        "single_thread": {"value": 64 ** 3 * c1s["steps"] / c1s["seconds"], "unit": UNIT,
+                                          "cores": 1,
+                                          "sample": f"{c1s['steps']} steps, one thread, median of 3 runs, "
+                                                    f"{c1s['seconds']:.2f} s each"}}}
 
 
 def ref_cufft(steps: int):
