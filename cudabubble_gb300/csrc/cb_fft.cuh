@@ -45,6 +45,30 @@ namespace cb {
 #define CB_FENCE() __threadfence()
 #endif
 
+// The threads a pass body runs on.  Cta: the whole CTA (threadIdx.x, __syncthreads).
+// Grp: one of the equal thread groups a CTA of the persistent batched kernel splits into
+// (mega.cuh), synchronised by its own named barrier `id` (1..15) over its n threads;
+// the groups are whole warps.  Every body and line transform takes one and uses only its
+// thread index, size and barrier.
+#if defined(__CUDA_ARCH__)
+#define CB_NAMED_SYNC(id, n) asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory")
+#elif defined(CB_EMULATION)
+#define CB_NAMED_SYNC(id, n) ::emu::named_sync(id, n)
+#else
+#define CB_NAMED_SYNC(id, n) ((void)(id), (void)(n))
+#endif
+struct Cta {
+    __device__ __forceinline__ int tid() const { return threadIdx.x; }
+    __device__ __forceinline__ int size() const { return blockDim.x; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+struct Grp {
+    int id, n, t;  // named barrier, threads, this thread's index in the group
+    __device__ __forceinline__ int tid() const { return t; }
+    __device__ __forceinline__ int size() const { return n; }
+    __device__ __forceinline__ void sync() const { CB_NAMED_SYNC(id, n); }
+};
+
 // ---------------------------------------------------------------- complex
 template <class T> struct CT;
 template <> struct CT<float> { using type = float2; };
@@ -307,11 +331,11 @@ struct TripleRows {
 
 // NT: natural in -> transposed out.  Lines l in [0, nlines) at buf + off(l),
 // element stride es.  All NTHR threads of the block call it; caller syncs after.
-template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
-__device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* tw, const C* twlo) {
+template <int L, bool INV, int NTHR, int NLINES, class C, class OFF, class G = Cta>
+__device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* tw, const C* twlo, const G& g = G()) {
     constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
-    const int tid = threadIdx.x;
+    const int tid = g.tid();
     if constexpr (R2 == 1) {
         for (int l = tid; l < nlines; l += NTHR) {
             C a[R1];
@@ -337,7 +361,7 @@ __device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* t
             p[k1 * R2 * es] = v;
         }
     }
-    __syncthreads();
+    g.sync();
     // phase B: for each (line, k1) DFT_R2 over j2 of the contiguous block at R2*k1
     for (int it = tid; it < nlines * R1; it += NTHR) {
         const int l = it % nlines, k1 = it / nlines;
@@ -354,13 +378,13 @@ __device__ __forceinline__ void fft_lines_NT(C* buf, OFF off, int es, const C* t
 
 // TN: transposed in -> natural out (input element j = j1 + R1 j2 sits at
 // slot j2 + R2 j1, exactly where an NT transform leaves element j).
-template <int L, bool INV, int NTHR, int NLINES, class C, class OFF>
-__device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* tw, const C* twlo) {
+template <int L, bool INV, int NTHR, int NLINES, class C, class OFF, class G = Cta>
+__device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* tw, const C* twlo, const G& g = G()) {
     constexpr int nlines = NLINES;
     constexpr int R1 = Plan<L>::R1, R2 = Plan<L>::R2;
-    const int tid = threadIdx.x;
+    const int tid = g.tid();
     if constexpr (R2 == 1) {
-        fft_lines_NT<L, INV, NTHR, NLINES, C, OFF>(buf, off, es, tw, twlo);
+        fft_lines_NT<L, INV, NTHR, NLINES, C, OFF, G>(buf, off, es, tw, twlo, g);
     } else {
     // phase A: for each (line, j1) DFT_R2 over j2 (contiguous block at R2*j1), twiddle W_L^{j1 k2}
     for (int it = tid; it < nlines * R1; it += NTHR) {
@@ -376,7 +400,7 @@ __device__ __forceinline__ void fft_lines_TN(C* buf, OFF off, int es, const C* t
             p[k2 * es] = v;
         }
     }
-    __syncthreads();
+    g.sync();
     // phase B: for each (line, k2) DFT_R1 over j1 at stride R2 -> X[k2 + R2 k1] at the same slots
     for (int it = tid; it < nlines * R2; it += NTHR) {
         const int l = it % nlines, k2 = it / nlines;
@@ -427,28 +451,29 @@ __device__ __forceinline__ double warp_sum(double v) {
 // whole block: strided loads, a warp-shuffle tree, then the per-warp sums.
 // The result is valid in thread 0.  Keeps the dependent FP64 chain short; a
 // single thread walking hundreds of partials dominated the kernels' tails.
-template <int NV>
-__device__ __forceinline__ void block_sum_parts(const double* part, int nparts, double* out, double* red) {
+template <int NV, class G = Cta>
+__device__ __forceinline__ void block_sum_parts(const double* part, int nparts, double* out, double* red,
+                                                const G& g = G()) {
     double v[NV];
 #pragma unroll
     for (int j = 0; j < NV; ++j) v[j] = 0.0;
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    for (int i = g.tid(); i < nparts; i += g.size()) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) v[j] += __ldcg(part + (size_t)NV * i + j);
     }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const int lane = g.tid() & 31, w = g.tid() >> 5, nw = (g.size() + 31) >> 5;
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
     }
-    __syncthreads();
+    g.sync();
     if (lane == 0) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) red[j * 32 + w] = v[j];
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    g.sync();
+    if (g.tid() == 0) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
             double s = 0.0;
@@ -460,12 +485,12 @@ __device__ __forceinline__ void block_sum_parts(const double* part, int nparts, 
 
 // Block-wide sum of NV values (FF pairs or doubles); the FP64 result is valid
 // in thread 0.  `red` must hold 32*NV doubles of shared memory.
-template <int NV, class V>
-__device__ __forceinline__ void block_sum(V* v, double* out, double* red) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+template <int NV, class V, class G = Cta>
+__device__ __forceinline__ void block_sum(V* v, double* out, double* red, const G& g = G()) {
+    const int lane = g.tid() & 31, w = g.tid() >> 5, nw = (g.size() + 31) >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
-    __syncthreads();
+    g.sync();
     if (lane == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
@@ -473,8 +498,8 @@ __device__ __forceinline__ void block_sum(V* v, double* out, double* red) {
             else red[i * 32 + w] = (double)v[i];
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    g.sync();
+    if (g.tid() == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
             double s = 0.0;

@@ -13,8 +13,9 @@ bool mega_size_ok(int n) {
 }
 
 template <int N> constexpr size_t mega_body_bytes() {
-    constexpr size_t z = z_smem_bytes<float, N, kMegaZTX>();
-    constexpr size_t xy = mega_cluster_xy(N) ? xyc_smem_bytes<float, N>() : xy_smem_bytes<float, N>(2);
+    constexpr size_t z = (kMegaThreads / kMegaZThreads) * mega_align(z_smem_bytes<float, N, kMegaZTX>());
+    constexpr size_t xy = mega_cluster_xy(N) ? xyc_smem_bytes<float, N>()
+                                             : (kMegaThreads / mega_xy_threads(N)) * mega_align(xy_smem_bytes<float, N>(2));
     return z > xy ? z : xy;
 }
 

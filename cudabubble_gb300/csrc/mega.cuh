@@ -1,12 +1,14 @@
 // The persistent batched attempt (FP32 form, ETD-RK2): one launch of two-CTA clusters
 // runs one attempt of every instance of a batched pool by walking the work list of
 // mega.h.  The units run the same pass bodies as the one-pass kernels (z_body,
-// xyc_body, xy_body, prologue_body with PDL = false), on 512-thread CTAs:
-//   z tiles of 32 columns (one CTA each; the one-pass z kernel takes 16 columns on 256
-//   threads), planes from 64^2 on both CTAs of the cluster, smaller planes one per CTA.
-// Each instance keeps its own dt and decision, so its result does not depend on the
-// other instances of the pool; it differs from the per-class graph only in the
-// summation order of its partial sums (tile and thread shapes).
+// xyc_body, xy_body, prologue_body with PDL = false) on 512-thread CTAs: z tiles and
+// planes below 64^2 on thread groups of the one-pass kernels' shapes (two 16-column,
+// 256-thread z tiles a CTA; two 256-thread or four 128-thread planes), each group on its
+// own named barrier and slice of shared memory; planes from 64^2 on both CTAs of the
+// cluster (512 threads a CTA; the one-pass kernel takes 256 at 64^2).  Each instance
+// keeps its own dt and decision, so its result does not depend on the other instances of
+// the pool; it is bitwise that of the per-class graph except for 64^2 planes, whose sums
+// differ in summation order.
 //
 // Hand-over: rank 0 of a cluster claims the next unit from the shared counter while
 // the current one runs and leaves it in one of two slots of its shared memory; a
@@ -39,19 +41,33 @@ namespace cb {
 #define CB_MEGA_SPIN (1 << 20)
 #endif
 
-template <int N> __device__ __noinline__ void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm) {
+__host__ __device__ constexpr size_t mega_align(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// z tile `tile` on thread group j of the CTA (256 threads, its own slice of shared memory)
+template <int N>
+__device__ __noinline__ void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm, int j) {
     ZArgs za = {};
     za.mode = mode;
     za.role = mode == Z_ETD2_S1 ? R_WORK : R_CAND;
-    z_body<float, N, kMegaZTX, kMegaThreads, ZG_ETD2, 0, false>(I, tile, za, sm);
+    const Grp g{1 + j, kMegaZThreads, (int)threadIdx.x - j * kMegaZThreads};
+    constexpr size_t bytes = mega_align(z_smem_bytes<float, N, kMegaZTX>());
+    z_body<float, N, kMegaZTX, kMegaZThreads, ZG_ETD2, 0, false>(I, tile, za, sm + j * bytes, g);
 }
 
-template <int N> __device__ __noinline__ void mega_xy(const InstT<float>& I, int plane, int role, unsigned char* sm) {
+// plane `plane` on the cluster (from 64^2), or on thread group j of the CTA
+template <int N>
+__device__ __noinline__ void mega_xy(const InstT<float>& I, int plane, int role, unsigned char* sm, int j) {
     XYArgs xa = {};
     xa.mode = XY_FUSED;
     xa.role = role;
-    if constexpr (mega_cluster_xy(N)) xyc_body<float, N, kMegaThreads, 0, false>(I, plane, xa, sm);
-    else xy_body<float, N, kMegaThreads, 2, 0, false>(I, plane, xa, sm);
+    if constexpr (mega_cluster_xy(N)) {
+        xyc_body<float, N, kMegaThreads, 0, false>(I, plane, xa, sm);
+    } else {
+        constexpr int NT = mega_xy_threads(N);
+        const Grp g{1 + j, NT, (int)threadIdx.x - j * NT};
+        constexpr size_t bytes = mega_align(xy_smem_bytes<float, N>(2));
+        xy_body<float, N, NT, 2, 0, false>(I, plane, xa, sm + j * bytes, g);
+    }
 }
 
 __device__ __noinline__ void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, unsigned char* head) {
@@ -114,30 +130,26 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
             case MP_Z1:
             case MP_Z2: {
                 const int mode = task.phase == MP_Z1 ? Z_ETD2_S1 : Z_ETD2_S2;
-                for (int j = 0; j < kMegaZPer; ++j) {
-                    if (j) __syncthreads();  // the last tile's reads of shared memory are done
-                    const int tile = part * kMegaZPer + j;
-                    switch (n) {
-#define CASE(N) case N: mega_z<N>(I, tile, mode, sm); break;
-                        CB_MEGA_SIZES(CASE)
+                constexpr int G = kMegaThreads / kMegaZThreads;
+                const int j = tid / kMegaZThreads;
+                switch (n) {
+#define CASE(N) case N: mega_z<N>(I, part * G + j, mode, sm, j); break;
+                    CB_MEGA_SIZES(CASE)
 #undef CASE
-                        default: break;
-                    }
+                    default: break;
                 }
                 break;
             }
             default: {  // MP_XYW, MP_XYC
                 const int role = task.phase == MP_XYW ? R_WORK : R_CAND;
-                const int per = mega_cluster_xy(n) ? 1 : kMegaXYPer;
-                for (int j = 0; j < per; ++j) {
-                    if (j) __syncthreads();  // the last plane's reads of shared memory are done
-                    const int plane = mega_cluster_xy(n) ? task.unit : part * kMegaXYPer + j;
-                    switch (n) {
-#define CASE(N) case N: mega_xy<N>(I, plane, role, sm); break;
-                        CB_MEGA_SIZES(CASE)
+                const int G = kMegaThreads / mega_xy_threads(n);
+                const int j = mega_cluster_xy(n) ? 0 : tid / mega_xy_threads(n);
+                const int plane = mega_cluster_xy(n) ? task.unit : part * G + j;
+                switch (n) {
+#define CASE(N) case N: mega_xy<N>(I, plane, role, sm, j); break;
+                    CB_MEGA_SIZES(CASE)
 #undef CASE
-                        default: break;
-                    }
+                    default: break;
                 }
                 break;
             }

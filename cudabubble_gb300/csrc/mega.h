@@ -4,9 +4,11 @@
 //
 // An attempt of one instance is five phases, each a set of units:
 //   MP_PRO  prologue and coefficient-table fill      (units of two 512-thread blocks)
-//   MP_Z1   z pass, stage 1                          (units of two 32-column tiles)
+//   MP_Z1   z pass, stage 1                          (units of four 16-column tiles, two a
+//                                                     CTA on 256-thread groups)
 //   MP_XYW  fused xy pass of the work stage           (a plane on both CTAs of a cluster
-//                                                     from 64^2, else two planes)
+//                                                     from 64^2, else 4 or 8 planes on
+//                                                     256- or 128-thread groups)
 //   MP_Z2   z pass, stage 2                          (as MP_Z1)
 //   MP_XYC  fused xy pass of the candidate, then the decision (the CTA that ends the
 //           phase runs it)
@@ -30,9 +32,9 @@ enum MegaPhase { MP_PRO = 0, MP_Z1 = 1, MP_XYW = 2, MP_Z2 = 3, MP_XYC = 4, MP_N 
 struct MegaTask {
     int phase;  // MegaPhase
     int inst;   // index into MegaArgs::insts
-    int unit;   // CTA rank r of the cluster runs part 2 unit + r (a plane: the unit itself
-                // on the cluster pass), i.e. z tiles or one-CTA planes k PER + j, j < PER,
-                // of k = 2 unit + r
+    int unit;   // CTA rank r of the cluster runs part k = 2 unit + r: on the cluster xy pass
+                // the plane `unit` itself; else its thread group j runs z tile or plane
+                // k G + j of the G groups a CTA holds
     int size;   // grid edge of the phase's transform (nz for z, nx for xy); bit 16: the
                 // class's accurate-coefficient mode
 };
@@ -48,23 +50,16 @@ struct MegaArgs {
     int pad;
 };
 
-// z tiles, and planes of the one-CTA plane pass, that one CTA runs in one unit (build-time
-// schedule knobs)
-#ifndef CB_MEGA_ZPER
-#define CB_MEGA_ZPER 1
-#endif
-#ifndef CB_MEGA_XYPER
-#define CB_MEGA_XYPER 1
-#endif
-constexpr int kMegaZPer = CB_MEGA_ZPER, kMegaXYPer = CB_MEGA_XYPER;
+constexpr int kMegaThreads = 512;   // threads of every CTA
+constexpr int kMegaZTX = 16;        // z tile: the one-pass kernel's 16 columns on 256 threads,
+constexpr int kMegaZThreads = 256;  // two tiles side by side in a CTA
+constexpr int kMegaHead = 128;      // dynamic shared-memory bytes before the bodies' region
+constexpr int kMegaProRows = 1024;  // coefficient-table entries per prologue unit (two blocks)
 
-constexpr int kMegaThreads = 512;  // threads of every CTA: one plane half, one z tile, ...
-constexpr int kMegaZTX = 32;       // z-tile columns of one CTA (16 threads per column)
-constexpr int kMegaHead = 128;     // dynamic shared-memory bytes before the bodies' region
-constexpr int kMegaProRows = 1024; // coefficient-table entries per prologue unit (two blocks)
-
-// planes of n^2 run on two-CTA clusters (both CTAs of a unit), smaller ones one per CTA
+// planes of n^2 run on two-CTA clusters (both CTAs of a unit); smaller ones side by side
+// in a CTA, each on the thread count of the one-pass kernel (128 threads to 32^2, else 256)
 __host__ __device__ constexpr bool mega_cluster_xy(int n) { return n >= 64; }
+__host__ __device__ constexpr int mega_xy_threads(int n) { return n <= 32 ? 128 : 256; }
 
 // one size class of the pool: instances [first, first + cap) of the instance table
 struct MegaClass {
@@ -79,8 +74,14 @@ inline int mega_units(const MegaClass& c, int ph) {
     switch (ph) {
         case MP_PRO: return std::max(1, (kmax + 1 + kMegaProRows - 1) / kMegaProRows);
         case MP_Z1:
-        case MP_Z2: return (ztiles + 2 * kMegaZPer - 1) / (2 * kMegaZPer);
-        default: return mega_cluster_xy(c.nx) ? c.nz : (c.nz + 2 * kMegaXYPer - 1) / (2 * kMegaXYPer);
+        case MP_Z2: {  // two CTAs of two tiles
+            const int per = 2 * (kMegaThreads / kMegaZThreads);
+            return (ztiles + per - 1) / per;
+        }
+        default: {  // a plane on the cluster, or two CTAs of side-by-side planes
+            const int per = 2 * (kMegaThreads / mega_xy_threads(c.nx));
+            return mega_cluster_xy(c.nx) ? c.nz : (c.nz + per - 1) / per;
+        }
     }
 }
 

@@ -55,15 +55,15 @@ __device__ inline void finalize_xy(const Params& p, Ctrl* ctrl, const double* su
 // Per-CTA partial sums (slot `slot` of `nslots`) of (u^2 - 1)^2, f^2 and, with
 // NV = 4 (XY_FUSED), of the partials G'' and w; then the last CTA of the
 // instance finalises the role's scalars; all threads call.
-template <class T, int NV = 2, class V>
+template <class T, int NV = 2, class V, class G = Cta>
 __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Params& p, int slot, int nslots, V* vv,
-                                        double* red, int role, bool full) {
+                                        double* red, int role, bool full, const G& g = G()) {
     static_assert(NV == 2 || NV == 4, "two or four sums");
     double v[NV];
-    block_sum<NV>(vv, v, red);
+    block_sum<NV>(vv, v, red, g);
     double* part = I.part_xy;
     int* last = reinterpret_cast<int*>(red + 128);
-    if (threadIdx.x == 0) {
+    if (g.tid() == 0) {
         part[4 * slot + 1] = v[0];
         part[4 * slot + 2] = v[1];
         if constexpr (NV == 4) {
@@ -77,12 +77,12 @@ __device__ inline void xy_sums_finalize(const InstT<T>& I, Ctrl* ctrl, const Par
         const unsigned done_blocks = atomicAdd(&ctrl->cnt_xy[role], 1u);
         *last = done_blocks == (unsigned)(nslots - 1);
     }
-    __syncthreads();
+    g.sync();
     if (*last) {  // the last CTA of this instance finalises, with all its threads
         CB_FENCE();
         double sums[4];
-        block_sum_parts<4>(part, nslots, sums, red);
-        if (threadIdx.x == 0) {
+        block_sum_parts<4>(part, nslots, sums, red, g);
+        if (g.tid() == 0) {
             finalize_xy(p, ctrl, sums, role, full);
             ctrl->cnt_xy[role] = 0u;
         }
@@ -114,8 +114,9 @@ __device__ __forceinline__ void nl_outputs(const InstT<T>& I, const Ctrl* c, int
 // Plane z of instance I on this CTA, all NT threads: the body of xy_kernel (one plane per
 // CTA, PDL = true: programmatic launch) and of the persistent batched kernel (mega.cuh,
 // PDL = false).
-template <class T, int NX, int NT, int NF, int NQ = 0, bool PDL = true>
-__device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XYArgs a, unsigned char* smem_raw) {
+template <class T, int NX, int NT, int NF, int NQ = 0, bool PDL = true, class G = Cta>
+__device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XYArgs a, unsigned char* smem_raw,
+                                        const G& g = G()) {
     using C = cplx<T>;
     constexpr int M = NX / 2, NY = NX, NC = M + 1;
     constexpr int nf = NF;
@@ -124,7 +125,7 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
     if constexpr (PDL) CB_PDL_TRIGGER();
     Ctrl* ctrl = I.ctrl;
     const Params& p = I.p;
-    const int tid = threadIdx.x;
+    const int tid = g.tid();
     if (z >= p.nz) return;
     C* S = reinterpret_cast<C*>(smem_raw);  // [NY][pitch]
     C* Qb = S + NY * pitch;                 // q (NQ = 1)
@@ -170,7 +171,7 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
             const double2 v = reinterpret_cast<const double2*>(src + (size_t)y * NX)[m];
             S[tpos<NY>(y) * pitch + tpos<M>(m)] = cmk<C>((T)v.x, (T)v.y);
         }
-        __syncthreads();
+        g.sync();
     } else {
         const C* P0;
         const C* P2 = nullptr;
@@ -242,10 +243,10 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
                 if (b0 + j < ITER && it < NY * M) put(it, v[j], w[j], vN[j], wN[j]);
             }
         }
-        __syncthreads();
+        g.sync();
         // ---- y inverse (natural in, transposed out) on nf*M columns
-        fft_lines_NT<NY, true, NT, nf * M>(S, LinearLines{1}, pitch, twY, twYl);
-        __syncthreads();
+        fft_lines_NT<NY, true, NT, nf * M>(S, LinearLines{1}, pitch, twY, twYl, g);
+        g.sync();
         // ---- x C2R: half-length pre-processing, then inverse M-point FFT per row
         const PairRows<NY, pitch, M> rows;
         for (int it = tid; it < nf * NY * (M / 2 + 1); it += NT) {
@@ -269,9 +270,9 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
                 }
             }
         }
-        __syncthreads();
-        fft_lines_NT<M, true, NT, nf * NY>(S, rows, 1, twM, twMl);
-        __syncthreads();
+        g.sync();
+        fft_lines_NT<M, true, NT, nf * NY>(S, rows, 1, twM, twMl, g);
+        g.sync();
 
         if (a.mode == XY_INV_PLAIN) {
             double* dst = a.rout + (size_t)z * NY * NX;
@@ -290,7 +291,7 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
             T* lam = reinterpret_cast<T*>(red);
             const bool euler = p.method == M_EULER;
             if (tid == 0) nonlin_lambdas<T>(p, ctrl, a.role, lam);
-            __syncthreads();
+            g.sync();
             const T g_c = lam[0];
             const T g_f = lam[1];
             for (int it = tid; it < NY * M; it += NT) {
@@ -304,7 +305,7 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
                 *pu = g;
                 *pl = h;
             }
-            __syncthreads();
+            g.sync();
         } else if (a.mode == XY_FUSED) {
             // sums of the state and its lambda-free partials G'', w in one sweep
             const bool euler = p.method == M_EULER;
@@ -356,8 +357,8 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
             }
             auto pv = as.part();
             decltype(pv) vv[4] = {pv, af.part(), ag.part(), ah.part()};
-            xy_sums_finalize<T, 4>(I, ctrl, p, z, p.nz, vv, red, a.role, true);
-            __syncthreads();
+            xy_sums_finalize<T, 4>(I, ctrl, p, z, p.nz, vv, red, a.role, true, g);
+            g.sync();
         } else {
             // reductions (XY_REDUCE_FULL / XY_REDUCE_S)
             const bool full = a.mode == XY_REDUCE_FULL;
@@ -371,7 +372,7 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
             }
             auto pv = as.part();
             decltype(pv) vv[2] = {pv, af.part()};
-            xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, full);
+            xy_sums_finalize<T>(I, ctrl, p, z, p.nz, vv, red, a.role, full, g);
             return;
         }
     }
@@ -381,9 +382,9 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
     const PairRows<NY, pitch, M> rows;
     const TripleRows<NY, pitch, M, NY * pitch, QX> rows3;
     auto xrow = [&](int l) { return NQ ? rows3(l) : rows(l); };
-    if constexpr (NQ == 1) fft_lines_TN<M, false, NT, 3 * NY>(S, rows3, 1, twM, twMl);
-    else fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl);
-    __syncthreads();
+    if constexpr (NQ == 1) fft_lines_TN<M, false, NT, 3 * NY>(S, rows3, 1, twM, twMl, g);
+    else fft_lines_TN<M, false, NT, nfo * NY>(S, rows, 1, twM, twMl, g);
+    g.sync();
     for (int it = tid; it < nfo * NY * (M / 2 + 1); it += NT) {
         const int l = it % (nfo * NY), k = it / (nfo * NY);
         C* row = S + xrow(l);
@@ -406,13 +407,13 @@ __device__ __forceinline__ void xy_body(const InstT<T>& I, const int z, const XY
             }
         }
     }
-    __syncthreads();
-    fft_lines_TN<NY, false, NT, NF * M>(S, LinearLines{1}, pitch, twY, twYl);
+    g.sync();
+    fft_lines_TN<NY, false, NT, NF * M>(S, LinearLines{1}, pitch, twY, twYl, g);
     if constexpr (NQ == 1) {
-        __syncthreads();
-        fft_lines_TN<NY, false, NT, M>(Qb, LinearLines{1}, QX, twY, twYl);
+        g.sync();
+        fft_lines_TN<NY, false, NT, M>(Qb, LinearLines{1}, QX, twY, twYl, g);
     }
-    __syncthreads();
+    g.sync();
 
     // ---- store (natural ky, kx), unpacking the kx = 0 / nx/2 column pair
     C* outA;
@@ -493,7 +494,7 @@ __global__ void __launch_bounds__(NT) xy_kernel(const InstT<T>* __restrict__ ins
     xy_body<T, NX, NT, NF, NQ, true>(insts[blockIdx.y], blockIdx.x, a, smem_raw);
 }
 
-template <class T, int NX> constexpr size_t xy_smem_bytes(int nf, int nq = 0) {
+template <class T, int NX> __host__ __device__ constexpr size_t xy_smem_bytes(int nf, int nq = 0) {
     constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
     return sizeof(cplx<T>) * ((size_t)NX * (nf * (NX / 2) + 1) + (nq ? (size_t)NX * (NX / 2 + 1) : 0) +
                               ntw * (NX / 2 + NX + NX)) +

@@ -138,9 +138,9 @@ __host__ __device__ constexpr int zgroup_of(int mode) {
 // NQ = 1 (FP32 stage groups with spontaneous curvature): the stage's third partial q is
 // transformed with A and B and takes B's multiplier, N-hat = (A-hat + beta cx kz^2 (B-hat +
 // q-hat)) / N, while f-hat keeps being rebuilt from B-hat alone
-template <class T, int NZ, int TX, int NT, int MG, int NQ = 0, bool PDL = true>
+template <class T, int NZ, int TX, int NT, int MG, int NQ = 0, bool PDL = true, class G = Cta>
 __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const ZArgs a,
-                                       unsigned char* smem_raw) {
+                                       unsigned char* smem_raw, const G& g = G()) {
     constexpr bool g2 = MG == ZG_ETD2, g4 = MG == ZG_ETD4, ge = MG == ZG_EULER, gp = MG == ZG_PLAIN;
     using C = cplx<T>;
     if constexpr (PDL) CB_PDL_TRIGGER();
@@ -149,7 +149,7 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
     const int nc = p.nc, ny = p.ny, nx = p.nx;
     const int Mc = ny * nc;
     const int m0 = tile * TX;
-    const int tid = threadIdx.x;
+    const int tid = g.tid();
     if (m0 >= Mc) return;
     const void* g_a[2] = {I.G[0][0], I.G[1][0]};
     const void* g_b[2] = {I.G[0][1], I.G[1][1]};
@@ -244,10 +244,10 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
                 }
             }
         }
-        __syncthreads();
-        if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw, twl);
-        else fft_lines_NT<NZ, false, NT, TX>(S, LinearLines{1}, W, tw, twl);
-        __syncthreads();
+        g.sync();
+        if (two) fft_lines_NT<NZ, false, NT, W>(S, LinearLines{1}, W, tw, twl, g);
+        else fft_lines_NT<NZ, false, NT, TX>(S, LinearLines{1}, W, tw, twl, g);
+        g.sync();
     }
 
     const PC<T> k(p);
@@ -278,7 +278,7 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
     C* Nb = reinterpret_cast<C*>(I.Nb);
     void* ah = I.ahat;
     const T* coef = I.coef + (size_t)ctrl->tab_cur * (size_t)(p.kmax + 1) * 8;
-    __syncthreads();
+    g.sync();
     const T dtga = bc[0];
     const T g_f = sizeof(T) == 4 ? bc[2] : (T)0;  // bc[1], the lambda1 constant, enters n0
     const T n0 = sizeof(T) == 4 ? bc[3] : (T)0;
@@ -560,11 +560,11 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
             S[r * W + TX + c] = cmk<C>(-k.k_cx.mul(kk * un.x), -k.k_cx.mul(kk * un.y));
         }
     }
-    __syncthreads();
+    g.sync();
     const bool two = a.mode != Z_INV_PLAIN;
-    if (two) fft_lines_TN<NZ, true, NT, 2 * TX>(S, LinearLines{1}, W, tw, twl);
-    else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw, twl);
-    __syncthreads();
+    if (two) fft_lines_TN<NZ, true, NT, 2 * TX>(S, LinearLines{1}, W, tw, twl, g);
+    else fft_lines_TN<NZ, true, NT, TX>(S, LinearLines{1}, W, tw, twl, g);
+    g.sync();
 
     // ---- store partials (natural z)
     C* o0;
@@ -589,8 +589,8 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
     else g0 += ag2.part();
     decltype(g0) vv[2] = {g0, al.part()};
     double v[2];
-    __syncthreads();  // red held dt*ga
-    block_sum<2>(vv, v, red);
+    g.sync();  // red held dt*ga
+    block_sum<2>(vv, v, red, g);
     double* part = I.part_z;
     int* last = reinterpret_cast<int*>(red + 64);
     if (tid == 0) {
@@ -600,11 +600,11 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
         const unsigned prev = atomicAdd(&ctrl->cnt_z[a.role], 1u);
         *last = prev == (unsigned)(ntiles - 1);
     }
-    __syncthreads();
+    g.sync();
     if (*last) {  // the last CTA of this instance finalises, with all its threads
         CB_FENCE();
         double sums[2];
-        block_sum_parts<2>(part, ntiles, sums, red);
+        block_sum_parts<2>(part, ntiles, sums, red, g);
         if (tid == 0) {
             ctrl->sc[a.role].grad2 = sums[0] * p.cx;
             if (a.mode == Z_EULER) ctrl->sc[a.role].lsq = sums[1];
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(NT, CB_Z_THREADS_PER_SM / NT) z_kernel(const I
     z_body<T, NZ, TX, NT, MG, NQ, true>(insts[blockIdx.y], blockIdx.x, a, smem_raw);
 }
 
-template <class T, int NZ, int TX, int NQ = 0> constexpr size_t z_smem_bytes() {
+template <class T, int NZ, int TX, int NQ = 0> __host__ __device__ constexpr size_t z_smem_bytes() {
     constexpr size_t ntw = sizeof(T) == 4 ? 2 : 1;
     return sizeof(cplx<T>) * ((size_t)NZ * (2 + NQ) * TX + ntw * NZ) + (32 * 2 + 2) * sizeof(double);
 }

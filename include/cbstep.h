@@ -228,8 +228,9 @@ int cb_batch_create(const cb_params* params, int n, cb_batch** out);
  * per-instance dependency counters, instead of one launch per pass and grid size.
  * FP32 form, ETD-RK2, grids of 32, 48, 64, 96 or 128 per edge, no spontaneous
  * curvature, the default xy path; otherwise CB_EUNSUPPORTED.  Each instance's
- * decisions are its own as in the default mode; its sums differ from the default
- * mode's only in summation order (the kernel's z tiles are 32 columns on 512 threads).
+ * decisions are its own as in the default mode, and its results are the default mode's
+ * bit for bit, except on 64^2 planes, which the kernel runs on 512-thread CTAs (256 in
+ * the default mode) and whose sums therefore differ in summation order.
  * A dependency wait that runs out of its bound makes cb_batch_run return CB_ETIMEOUT. */
 #define CB_BATCH_PERSISTENT 1
 int cb_batch_create_ex(const cb_params* params, int n, int flags, cb_batch** out);

@@ -69,6 +69,8 @@ struct Barrier {
 };
 struct Block {
     Barrier bar;
+    Barrier named[16];  // bar.sync id, n: the group barriers of the persistent batched kernel
+    Barrier warp[32];   // the warps' shuffles
     double* ex = nullptr;  // shuffle exchange, one slot per thread
     unsigned char* smem = nullptr;
     size_t smem_bytes = 0;
@@ -91,6 +93,24 @@ extern std::mutex g_atomic_mu;
 #define gridDim (::emu::g_gdim)
 
 inline void __syncthreads() { emu::t_blk->bar.wait(); }
+#define CB_EMULATION 1
+namespace emu {
+// named barrier `id` of this block over n threads: each generation takes the count of
+// its first arrival, as bar.sync does (the same id serves groups of different sizes)
+inline void named_sync(int id, int n) {
+    Barrier& b = t_blk->named[id];
+    std::unique_lock<std::mutex> lk(b.mu);
+    if (b.arrived == 0) b.alive = n;
+    const long g = b.gen;
+    if (++b.arrived == b.alive) {
+        b.arrived = 0;
+        ++b.gen;
+        b.cv.notify_all();
+    } else {
+        b.cv.wait(lk, [&] { return b.gen != g; });
+    }
+}
+}  // namespace emu
 inline void __threadfence() { std::atomic_thread_fence(std::memory_order_seq_cst); }
 template <class T> inline T __ldg(const T* p) { return *p; }
 template <class T> inline T __ldcg(const T* p) { return *p; }
@@ -103,10 +123,11 @@ inline unsigned atomicAdd(unsigned* p, unsigned v) {
 template <class T> inline T __shfl_xor_sync(unsigned, T v, int o) {
     emu::Block* b = emu::t_blk;
     const int t = (int)threadIdx.x;
+    emu::Barrier& w = b->warp[t >> 5];  // a warp-wide exchange, as on the device
     b->ex[t] = (double)v;
-    b->bar.wait();
+    w.wait();
     const T r = (T)b->ex[t ^ o];
-    b->bar.wait();
+    w.wait();
     return r;
 }
 inline float __fadd_rn(float a, float b) { return a + b; }

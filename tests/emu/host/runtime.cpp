@@ -56,6 +56,11 @@ void launch(dim3 grid, int nt, size_t smem, int clus, const std::function<void()
         for (int r = 0; r < clus; ++r) {
             blocks[r].bar.alive = nt;
             blocks[r].bar.arrived = 0;
+            for (auto& nb : blocks[r].named) nb.alive = nb.arrived = 0;
+            for (int w = 0; w < 32; ++w) {
+                blocks[r].warp[w].alive = std::max(0, std::min(32, nt - 32 * w));
+                blocks[r].warp[w].arrived = 0;
+            }
             memset(blocks[r].smem, 0xA5, smem);
         }
     };
@@ -74,6 +79,7 @@ void launch(dim3 grid, int nt, size_t smem, int clus, const std::function<void()
                     t_bid = dim3(bx + r, by);
                     body();
                     blocks[r].bar.drop();
+                    blocks[r].warp[(t % nt) >> 5].drop();
                     cl.bar.drop();
                     pool.wait();  // every thread is done with this cluster
                     if (t == 0) reset();

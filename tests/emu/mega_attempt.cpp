@@ -1,11 +1,12 @@
 // Test infrastructure (tests/test_kernel_emulation.py): one attempt of a small batched pool
 // through the persistent batched kernel (mega.cuh), run on the host by the CUDA emulation
 // in fake/ and checked by AddressSanitizer, against the same attempt through the one-pass
-// kernels with the persistent kernel's shapes (z tiles of 32 columns on 512 threads,
-// 512-thread plane passes).  Both run the same pass bodies, so every buffer and every
-// control field must come out bitwise the same; the persistent kernel's own parts (the
-// work list, the unit hand-over between the two CTAs of a cluster, the dependency
-// counters, the decision by the CTA that ends an instance's last phase) are what differ.
+// kernels with the persistent kernel's shapes (the one-pass z and one-CTA plane kernels'
+// own shapes, 512-thread CTAs for the cluster plane pass).  Both run the same pass bodies,
+// so every buffer and every control field must come out bitwise the same; the persistent
+// kernel's own parts (the work list, the unit hand-over between the two CTAs of a cluster,
+// the thread groups on named barriers, the dependency counters, the decision by the CTA
+// that ends an instance's last phase) are what differ.
 //
 // The pool: a 32^3 instance (planes one per CTA), a 64 x 64 x 16 instance (planes on
 // both CTAs of a cluster) and a 16^3 instance, each with its own synthetic state.  The
@@ -53,8 +54,8 @@ template <int N, int NZ> struct Inst {
             emu::launch(dim3(2 * NZ, 1), kMegaThreads, xyc_smem_bytes<T, N>(), 2,
                         [&] { xyc_fused_kernel<T, N, kMegaThreads>(d, a); });
         } else {
-            emu::launch(dim3(NZ, 1), kMegaThreads, xy_smem_bytes<T, N>(2), 1,
-                        [&] { xy_kernel<T, N, kMegaThreads, 2>(d, a); });
+            constexpr int NT = mega_xy_threads(N);
+            emu::launch(dim3(NZ, 1), NT, xy_smem_bytes<T, N>(2), 1, [&] { xy_kernel<T, N, NT, 2>(d, a); });
         }
     }
     void z(int mode, int role) {
@@ -63,8 +64,8 @@ template <int N, int NZ> struct Inst {
         za.mode = mode;
         za.role = role;
         const int nt = (N * h.p.nc + kMegaZTX - 1) / kMegaZTX;
-        emu::launch(dim3(nt, 1), kMegaThreads, z_smem_bytes<T, NZ, kMegaZTX>(), 1,
-                    [&] { z_kernel<T, NZ, kMegaZTX, kMegaThreads, ZG_ETD2>(d, za); });
+        emu::launch(dim3(nt, 1), kMegaZThreads, z_smem_bytes<T, NZ, kMegaZTX>(), 1,
+                    [&] { z_kernel<T, NZ, kMegaZTX, kMegaZThreads, ZG_ETD2>(d, za); });
     }
     // one ETD-RK2 attempt through the one-pass kernels
     void attempt() {
@@ -148,10 +149,13 @@ int main() {
     m.ticket = done.data() + need.size();
     m.err = &err;
     m.ntasks = (int)tasks.size();
+    // the kernel's dynamic shared memory for these sizes (kernels_mega.cu, mega_smem_bytes)
+    auto zb = [](size_t b) { return 2 * mega_align(b); };
+    auto xb = [](int n, size_t b) { return (size_t)(kMegaThreads / mega_xy_threads(n)) * mega_align(b); };
     size_t smem = 0;
-    smem = std::max(smem, std::max(z_smem_bytes<T, 32, kMegaZTX>(), xy_smem_bytes<T, 32>(2)));
-    smem = std::max(smem, std::max(z_smem_bytes<T, 16, kMegaZTX>(), xyc_smem_bytes<T, 64>()));
-    smem = std::max(smem, std::max(z_smem_bytes<T, 16, kMegaZTX>(), xy_smem_bytes<T, 16>(2)));
+    smem = std::max(smem, std::max(zb(z_smem_bytes<T, 32, kMegaZTX>()), xb(32, xy_smem_bytes<T, 32>(2))));
+    smem = std::max(smem, std::max(zb(z_smem_bytes<T, 16, kMegaZTX>()), xyc_smem_bytes<T, 64>()));
+    smem = std::max(smem, std::max(zb(z_smem_bytes<T, 16, kMegaZTX>()), xb(16, xy_smem_bytes<T, 16>(2))));
     smem += kMegaHead;
     emu::launch(dim3(2), kMegaThreads, smem, 2, [&] { mega_kernel(m); });
     int bad = 0;
