@@ -74,6 +74,11 @@ template <class T> struct PoolClass {
     cudaEvent_t fork = nullptr, join = nullptr;
 };
 
+// priorities of the batched pool's class streams (0: none; see build_graph)
+#ifndef CB_BATCH_PRIORITY
+#define CB_BATCH_PRIORITY 0
+#endif
+
 template <class T> class Pool {
    public:
     ~Pool() {
@@ -170,6 +175,29 @@ template <class T> class Pool {
         for (auto& c : cls) total += c.cap;
         CB_CK(cudaMallocHost(&h_sum, sizeof(SlotSummary) * (total > 0 ? total : 1)));
         if (persistent) return build_mega_graph();
+#if CB_BATCH_PRIORITY
+        // class streams with priorities by grid size, captured into the graph's kernel
+        // nodes: 1 = largest grid first (its pass chain is the attempt's critical path),
+        // 2 = smallest first
+        {
+            int lo = 0, hi = 0;
+            CB_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            std::vector<long long> sizes;
+            for (auto& c : cls) sizes.push_back((long long)c.nx * c.nx * c.nz);
+            std::sort(sizes.begin(), sizes.end());
+            sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+            const int levels = lo - hi + 1;
+            for (auto& c : cls) {
+                const long long sz = (long long)c.nx * c.nx * c.nz;
+                int rank = (int)(std::lower_bound(sizes.begin(), sizes.end(), sz) - sizes.begin());
+                if (CB_BATCH_PRIORITY == 1) rank = (int)sizes.size() - 1 - rank;
+                const int pri = hi + (int)((long long)rank * levels / (long long)sizes.size());
+                CB_CK(cudaStreamDestroy(c.s));
+                c.s = nullptr;
+                CB_CK(cudaStreamCreateWithPriority(&c.s, cudaStreamNonBlocking, std::min(pri, lo)));
+            }
+        }
+#endif
         cudaGraph_t gr = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t r = cudaSuccess;
@@ -200,19 +228,23 @@ template <class T> class Pool {
     int mega_clusters = 0, mega_tasks = 0;
 
     int mega_check() const {
-        if (!std::is_same<T, float>::value) return fail(CB_EUNSUPPORTED, "persistent batch: FP32 form only");
-        for (auto& c : cls) {
-            if (c.method != M_ETD2) return fail(CB_EUNSUPPORTED, "persistent batch: ETD-RK2 only");
-            if (c.curv) return fail(CB_EUNSUPPORTED, "persistent batch: no spontaneous curvature");
-            if (!mega_size_ok(c.nx) || !mega_size_ok(c.nz))
-                return fail(CB_EUNSUPPORTED, "persistent batch: grid %dx%dx%d not built into its kernel", c.nx, c.nx,
-                            c.nz);
-            const bool clus = mega_cluster_xy(c.nx);
-            if (c.split == XYP_SPLIT || (clus && c.split == XYP_SINGLE) || (!clus && c.split == XYP_CLUSTER))
-                return fail(CB_EUNSUPPORTED, "persistent batch: xy path %d of %d^2 planes not built into its kernel",
-                            c.split, c.nx);
+        if constexpr (!std::is_same<T, float>::value) {
+            return fail(CB_EUNSUPPORTED, "persistent batch: FP32 form only");
+        } else {
+            for (auto& c : cls) {
+                if (c.method != M_ETD2) return fail(CB_EUNSUPPORTED, "persistent batch: ETD-RK2 only");
+                if (c.curv) return fail(CB_EUNSUPPORTED, "persistent batch: no spontaneous curvature");
+                if (!mega_size_ok(c.nx) || !mega_size_ok(c.nz))
+                    return fail(CB_EUNSUPPORTED, "persistent batch: grid %dx%dx%d not built into its kernel", c.nx,
+                                c.nx, c.nz);
+                const bool clus = mega_cluster_xy(c.nx);
+                if (c.split == XYP_SPLIT || (clus && c.split == XYP_SINGLE) || (!clus && c.split == XYP_CLUSTER))
+                    return fail(CB_EUNSUPPORTED,
+                                "persistent batch: xy path %d of %d^2 planes not built into its kernel", c.split,
+                                c.nx);
+            }
+            return CB_OK;
         }
-        return CB_OK;
     }
 
     // the work list (phase-major, larger grids first), the per-phase completion counts,
