@@ -31,6 +31,13 @@
 
 namespace cb {
 
+// the unit bodies are separate functions (their registers are allocated one by one)
+#if defined(CB_EMULATION)
+#define CB_NOINLINE __attribute__((noinline))
+#else
+#define CB_NOINLINE __noinline__
+#endif
+
 // the grid edges the kernel is built for (each adds a z body and an xy body)
 #ifndef CB_MEGA_SIZES
 #define CB_MEGA_SIZES(X) X(32) X(48) X(64) X(96) X(128)
@@ -45,7 +52,7 @@ __host__ __device__ constexpr size_t mega_align(size_t b) { return (b + 15) & ~(
 
 // z tile `tile` on thread group j of the CTA (256 threads, its own slice of shared memory)
 template <int N>
-__device__ __noinline__ void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm, int j) {
+__device__ CB_NOINLINE void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm, int j) {
     ZArgs za = {};
     za.mode = mode;
     za.role = mode == Z_ETD2_S1 ? R_WORK : R_CAND;
@@ -56,7 +63,7 @@ __device__ __noinline__ void mega_z(const InstT<float>& I, int tile, int mode, u
 
 // plane `plane` on the cluster (from 64^2), or on thread group j of the CTA
 template <int N>
-__device__ __noinline__ void mega_xy(const InstT<float>& I, int plane, int role, unsigned char* sm, int j) {
+__device__ CB_NOINLINE void mega_xy(const InstT<float>& I, int plane, int role, unsigned char* sm, int j) {
     XYArgs xa = {};
     xa.mode = XY_FUSED;
     xa.role = role;
@@ -70,7 +77,7 @@ __device__ __noinline__ void mega_xy(const InstT<float>& I, int plane, int role,
     }
 }
 
-__device__ __noinline__ void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, unsigned char* head) {
+__device__ CB_NOINLINE void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, unsigned char* head) {
     ProState* s = reinterpret_cast<ProState*>(head + 16);
     int* last = reinterpret_cast<int*>(head + 12);
     prologue_body<float>(I, blk, nblk, accurate, 0, s, last);
@@ -78,7 +85,7 @@ __device__ __noinline__ void mega_pro(const InstT<float>& I, int blk, int nblk, 
 
 static_assert(sizeof(ProState) + 16 <= kMegaHead, "the prologue's shared state fits the head");
 
-__device__ __noinline__ void mega_decide(const InstT<float>& I) { decide_one(I, 0); }
+__device__ CB_NOINLINE void mega_decide(const InstT<float>& I) { decide_one(I, 0); }
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) mega_kernel(const MegaArgs a) {
     namespace cg = cooperative_groups;

@@ -74,11 +74,6 @@ template <class T> struct PoolClass {
     cudaEvent_t fork = nullptr, join = nullptr;
 };
 
-// priorities of the batched pool's class streams (0: none; see build_graph)
-#ifndef CB_BATCH_PRIORITY
-#define CB_BATCH_PRIORITY 0
-#endif
-
 template <class T> class Pool {
    public:
     ~Pool() {
@@ -175,29 +170,6 @@ template <class T> class Pool {
         for (auto& c : cls) total += c.cap;
         CB_CK(cudaMallocHost(&h_sum, sizeof(SlotSummary) * (total > 0 ? total : 1)));
         if (persistent) return build_mega_graph();
-#if CB_BATCH_PRIORITY
-        // class streams with priorities by grid size, captured into the graph's kernel
-        // nodes: 1 = largest grid first (its pass chain is the attempt's critical path),
-        // 2 = smallest first
-        {
-            int lo = 0, hi = 0;
-            CB_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-            std::vector<long long> sizes;
-            for (auto& c : cls) sizes.push_back((long long)c.nx * c.nx * c.nz);
-            std::sort(sizes.begin(), sizes.end());
-            sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
-            const int levels = lo - hi + 1;
-            for (auto& c : cls) {
-                const long long sz = (long long)c.nx * c.nx * c.nz;
-                int rank = (int)(std::lower_bound(sizes.begin(), sizes.end(), sz) - sizes.begin());
-                if (CB_BATCH_PRIORITY == 1) rank = (int)sizes.size() - 1 - rank;
-                const int pri = hi + (int)((long long)rank * levels / (long long)sizes.size());
-                CB_CK(cudaStreamDestroy(c.s));
-                c.s = nullptr;
-                CB_CK(cudaStreamCreateWithPriority(&c.s, cudaStreamNonBlocking, std::min(pri, lo)));
-            }
-        }
-#endif
         cudaGraph_t gr = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t r = cudaSuccess;

@@ -19,7 +19,6 @@
 #define __host__
 #define __global__
 #define __forceinline__ inline
-#define __noinline__ __attribute__((noinline))
 #define __launch_bounds__(...)
 #define __cluster_dims__(...)
 #define __align__(n) alignas(n)
