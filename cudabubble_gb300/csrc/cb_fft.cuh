@@ -49,7 +49,9 @@ namespace cb {
 // Grp: one of the equal thread groups a CTA of the persistent batched kernel splits into
 // (mega.cuh), synchronised by its own named barrier `id` (1..15) over its n threads;
 // the groups are whole warps.  Every body and line transform takes one and uses only its
-// thread index, size and barrier.
+// thread index, size and barrier.  Index and size are unsigned like threadIdx.x and
+// blockDim.x: with int the block sums compiled differently and the 128^2 fused plane pass
+// measured 1.2 % slower.
 #if defined(__CUDA_ARCH__)
 #define CB_NAMED_SYNC(id, n) asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory")
 #elif defined(CB_EMULATION)
@@ -58,14 +60,14 @@ namespace cb {
 #define CB_NAMED_SYNC(id, n) ((void)(id), (void)(n))
 #endif
 struct Cta {
-    __device__ __forceinline__ int tid() const { return threadIdx.x; }
-    __device__ __forceinline__ int size() const { return blockDim.x; }
+    __device__ __forceinline__ unsigned tid() const { return threadIdx.x; }
+    __device__ __forceinline__ unsigned size() const { return blockDim.x; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
 };
 struct Grp {
     int id, n, t;  // named barrier, threads, this thread's index in the group
-    __device__ __forceinline__ int tid() const { return t; }
-    __device__ __forceinline__ int size() const { return n; }
+    __device__ __forceinline__ unsigned tid() const { return (unsigned)t; }
+    __device__ __forceinline__ unsigned size() const { return (unsigned)n; }
     __device__ __forceinline__ void sync() const { CB_NAMED_SYNC(id, n); }
 };
 
