@@ -292,6 +292,14 @@ def plain_fp64(steps: int):
 PATH_NAMES = ["auto", "split", "single", "cluster"]
 
 
+def schedule_defines():
+    """The build-time launch schedule the library was compiled with (z tile, thread counts,
+    line splits): the schedule tuner's choice in cudabubble_gb300/schedule.txt, or
+    CB_NVCC_DEFINES."""
+    from cudabubble_gb300 import build
+    return " ".join(build.defines()) or "defaults"
+
+
 def batched(steps: int, tune: bool = False, persistent: bool = False):
     """Workload config 4 through cb_batch (FP32 form); with `tune`, the xy path of each
     size class is chosen by cb_autotune first, else by the size rule; `persistent`: one
@@ -316,6 +324,7 @@ def batched(steps: int, tune: bool = False, persistent: bool = False):
     return {"value": pts / (r["device_ms"] / 1e3), "unit": UNIT, "instances": len(plist),
             "grid_points": int(sum(p.nx * p.ny * p.nz for p in plist)), "steps_per_instance": steps,
             "xy_paths": {f"{k[0]}x{k[0]}x{k[1]}": PATH_NAMES[v] for k, v in tuned.items()} or "size rule",
+            "schedule": schedule_defines(),
             "attempts": r["attempts"], "device_ms": r["device_ms"],
             "what": "config 4: 64 vesicles, grids U{32,48,64,96,128}^3 (seed 4), alpha x U[0.6,0.95], ETD-RK2 "
                     "per-instance adaptive dt, FP32 form; "
