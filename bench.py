@@ -369,6 +369,7 @@ def served(duration_s: float, max_steps: int, tune: bool = False):
             "value": stats["point_steps"] / stats["wall_s"], "unit": UNIT, "wall_s": stats["wall_s"],
             "offered_point_steps_per_s": offered, "peak_bytes": stats["peak_bytes"],
             "xy_paths": {f"{k[0]}x{k[0]}x{k[1]}": PATH_NAMES[v] for k, v in tuned.items()} or "size rule",
+            "schedule": schedule_defines(),
             "what": f"config 5: the first {duration_s:g} s of a Poisson 200 req/s trace (seed 5), grids "
                     f"{{32..256}}^3 weighted 30/25/20/15/7/3 %, ETD-RK2 to |dE/E|<1e-8 (max {max_steps} steps), "
                     "150 GB budget, continuous batching (per-class streams, arenas carved up front), FP32 form; "
