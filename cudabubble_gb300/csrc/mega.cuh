@@ -10,18 +10,23 @@
 // the pool; it is bitwise that of the per-class graph except for 64^2 planes, whose sums
 // differ in summation order.
 //
-// Hand-over: rank 0 of a cluster claims the next unit from the shared counter while
-// the current one runs and leaves it in one of two slots of its shared memory; a
-// cluster barrier per unit hands it to rank 1 (which reads it through distributed
-// shared memory), so both CTAs run the same sequence of units and meet the same
-// cluster barriers inside the cluster xy body.
+// Hand-over: rank 0 of a cluster claims the next unit from the shared counter as the
+// current one starts, and its descriptor streams into shared memory (cp.async) under the
+// current unit's work.  Between units rank 0 checks the next unit's dependency, leaves
+// the unit and its descriptor in one of two slots of its shared memory, and a cluster
+// barrier hands them to rank 1 (which copies them through distributed shared memory).
+// Both CTAs run the same sequence of units and meet the same cluster barriers inside the
+// cluster xy body.  The instance pointers sit in shared memory from the start.
 //
-// Waits: thread 0 of a CTA polls the previous phase's completion counter of the unit's
-// instance with a bounded number of polls.  A wait that runs out counts in err and the
-// unit runs anyway (its results are then not used: the pool reports the attempt as
-// failed), so the control flow of the two CTAs of a cluster never parts.
+// Waits: rank 0's thread 0 polls the previous phase's completion counter of the unit's
+// instance with a bounded number of polls, then acquires; the cluster barrier passes that
+// on to rank 1.  A wait that runs out counts in err and the unit runs anyway (its results
+// are then not used: the pool reports the attempt as failed), so the control flow of the
+// two CTAs of a cluster never parts.
 #pragma once
 #include <cooperative_groups.h>
+
+#include <cstddef>
 
 #include "mega.h"
 #include "misc_kernels.cuh"
@@ -50,6 +55,40 @@ namespace cb {
 
 __host__ __device__ constexpr size_t mega_align(size_t b) { return (b + 15) & ~(size_t)15; }
 
+// the head of a CTA's dynamic shared memory
+struct MegaSlot {
+    unsigned t;  // the unit (>= ntasks: the walk is over)
+    int pad[3];
+    MegaTask task;
+};
+struct MegaHeadLayout {
+    MegaSlot slot[2];  // rank 0's hand-over slots (round parity)
+    MegaSlot cur;      // this CTA's unit of the round
+    MegaTask next;     // rank 0: the next unit's descriptor, streamed in under the current unit
+    int last;          // the prologue's last-block flag
+    int pad;
+    ProState pro;      // the prologue's block state
+    const InstT<float>* insts[kMegaInstCache];
+};
+static_assert(sizeof(MegaHeadLayout) <= kMegaHead, "the head fits");
+static_assert(offsetof(MegaHeadLayout, next) % 16 == 0, "cp.async target aligned");
+
+// a 16-byte global -> shared copy that completes asynchronously (this thread waits for it
+// with mega_copy_wait)
+__device__ __forceinline__ void mega_copy16(void* dst, const void* src) {
+#if defined(__CUDA_ARCH__)
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n\tcp.async.commit_group;" ::"r"(d), "l"(src) : "memory");
+#else
+    memcpy(dst, src, 16);
+#endif
+}
+__device__ __forceinline__ void mega_copy_wait() {
+#if defined(__CUDA_ARCH__)
+    asm volatile("cp.async.wait_all;" ::: "memory");
+#endif
+}
+
 // z tile `tile` on thread group j of the CTA (256 threads, its own slice of shared memory)
 template <int N>
 __device__ CB_NOINLINE void mega_z(const InstT<float>& I, int tile, int mode, unsigned char* sm, int j) {
@@ -77,13 +116,9 @@ __device__ CB_NOINLINE void mega_xy(const InstT<float>& I, int plane, int role, 
     }
 }
 
-__device__ CB_NOINLINE void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, unsigned char* head) {
-    ProState* s = reinterpret_cast<ProState*>(head + 16);
-    int* last = reinterpret_cast<int*>(head + 12);
-    prologue_body<float>(I, blk, nblk, accurate, 0, s, last);
+__device__ CB_NOINLINE void mega_pro(const InstT<float>& I, int blk, int nblk, int accurate, MegaHeadLayout* h) {
+    prologue_body<float>(I, blk, nblk, accurate, 0, &h->pro, &h->last);
 }
-
-static_assert(sizeof(ProState) + 16 <= kMegaHead, "the prologue's shared state fits the head");
 
 __device__ CB_NOINLINE void mega_decide(const InstT<float>& I) { decide_one(I, 0); }
 
@@ -93,46 +128,63 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     const int tid = threadIdx.x;
-    // head: [0], [1] the hand-over slots (read in rank 0's copy), [2] this CTA's unit
-    unsigned* box = reinterpret_cast<unsigned*>(smem_raw);
-    const unsigned* src = rank == 0 ? box : cl.map_shared_rank(box, 0);
+    MegaHeadLayout* h = reinterpret_cast<MegaHeadLayout*>(smem_raw);
+    const MegaSlot* src = rank == 0 ? h->slot : cl.map_shared_rank(h->slot, 0);
     unsigned char* sm = smem_raw + kMegaHead;
+    const int ncache = a.ninst < kMegaInstCache ? a.ninst : kMegaInstCache;
+    for (int i = tid; i < ncache; i += kMegaThreads) h->insts[i] = a.insts[i];
     unsigned claimed = 0;  // rank 0, thread 0: the unit of the next round
-    if (rank == 0 && tid == 0) claimed = atomicAdd(a.ticket, 1u);
+    if (rank == 0 && tid == 0) {
+        claimed = atomicAdd(a.ticket, 1u);
+        if (claimed < (unsigned)a.ntasks) h->next = a.tasks[claimed];
+    }
     for (int round = 0;; ++round) {
-        if (rank == 0 && tid == 0) box[round & 1] = claimed;
-        // the round's unit is in rank 0's slot; both CTAs are done with the last round
-        cl.sync();
-        if (tid == 0) box[2] = src[round & 1];
-        __syncthreads();
-        const unsigned t = box[2];
-        if (t >= (unsigned)a.ntasks) break;
-        if (rank == 0 && tid == 0) claimed = atomicAdd(a.ticket, 1u);  // under this round's work
-        const MegaTask task = a.tasks[t];
-        const int slot = task.inst * MP_N + task.phase;
-        if (tid == 0 && task.phase != MP_PRO) {
-            const volatile unsigned* d = a.done + slot - 1;
-            const volatile unsigned* failed = a.err;
-            const unsigned need = a.need[slot - 1];
-            int n = 0;
-            // once any wait of the launch has run out, none waits: the attempt is void and
-            // ends without a further bound's delay per unit
-            while (*d < need && *failed == 0u) {
-                if (++n > CB_MEGA_SPIN) {
-                    atomicAdd(a.err, 1u);
-                    break;
+        if (rank == 0 && tid == 0) {
+            // the round's unit, its descriptor and its dependency, checked before the hand-over
+            MegaSlot& s = h->slot[round & 1];
+            s.t = claimed;
+            if (claimed < (unsigned)a.ntasks) {
+                mega_copy_wait();
+                s.task = h->next;
+                if (s.task.phase != MP_PRO) {
+                    const int dep = s.task.inst * MP_N + s.task.phase - 1;
+                    const volatile unsigned* d = a.done + dep;
+                    const volatile unsigned* failed = a.err;
+                    const unsigned need = a.need[dep];
+                    int n = 0;
+                    // once any wait of the launch has run out, none waits: the attempt is void
+                    // and ends without a further bound's delay per unit
+                    while (*d < need && *failed == 0u) {
+                        if (++n > CB_MEGA_SPIN) {
+                            atomicAdd(a.err, 1u);
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                    CB_FENCE();  // the previous phase's writes before this unit's reads
                 }
-                __nanosleep(64);
             }
-            CB_FENCE();  // the previous phase's writes before this unit's reads
         }
+        // the round's unit is in rank 0's slot, its dependency met; both CTAs are done with
+        // the last round.  The barrier's release / acquire passes rank 0's acquisition of the
+        // previous phase's writes on to rank 1.
+        cl.sync();
+        if (tid == 0) h->cur = src[round & 1];
         __syncthreads();
-        const InstT<float>& I = *a.insts[task.inst];
+        const unsigned t = h->cur.t;
+        if (t >= (unsigned)a.ntasks) break;
+        const MegaTask task = h->cur.task;
+        if (rank == 0 && tid == 0) {  // claim the next unit and stream its descriptor in
+            claimed = atomicAdd(a.ticket, 1u);
+            if (claimed < (unsigned)a.ntasks) mega_copy16(&h->next, a.tasks + claimed);
+        }
+        const int slot = task.inst * MP_N + task.phase;
+        const InstT<float>& I = task.inst < ncache ? *h->insts[task.inst] : *a.insts[task.inst];
         const int n = task.size & 0xffff;
         const int part = 2 * task.unit + rank;
         switch (task.phase) {
             case MP_PRO:
-                mega_pro(I, part, (int)a.need[slot], task.size >> 16, smem_raw);
+                mega_pro(I, part, (int)a.need[slot], task.size >> 16, h);
                 break;
             case MP_Z1:
             case MP_Z2: {

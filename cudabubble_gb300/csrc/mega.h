@@ -47,13 +47,14 @@ struct MegaArgs {
     unsigned* ticket;                  // next unclaimed unit (zeroed before)
     unsigned* err;                     // waits that ran out of their bound (0 when healthy)
     int ntasks;
-    int pad;
+    int ninst;                         // entries of insts
 };
 
 constexpr int kMegaThreads = 512;   // threads of every CTA
 constexpr int kMegaZTX = 16;        // z tile: the one-pass kernel's 16 columns on 256 threads,
 constexpr int kMegaZThreads = 256;  // two tiles side by side in a CTA
-constexpr int kMegaHead = 128;      // dynamic shared-memory bytes before the bodies' region
+constexpr int kMegaInstCache = 256; // instance pointers a CTA keeps in shared memory
+constexpr int kMegaHead = 2304;     // dynamic shared-memory bytes before the bodies' region
 constexpr int kMegaProRows = 1024;  // coefficient-table entries per prologue unit (two blocks)
 
 // planes of n^2 run on two-CTA clusters (both CTAs of a unit); smaller ones side by side

@@ -255,6 +255,7 @@ template <class T> class Pool {
         a.ticket = m_done + need.size();
         a.err = m_err;
         a.ntasks = mega_tasks;
+        a.ninst = (int)ptrs.size();
         cudaGraph_t gr = nullptr;
         CB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t r = cudaMemsetAsync(m_done, 0, sizeof(unsigned) * (need.size() + 1), st);

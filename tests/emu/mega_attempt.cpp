@@ -149,6 +149,7 @@ int main() {
     m.ticket = done.data() + need.size();
     m.err = &err;
     m.ntasks = (int)tasks.size();
+    m.ninst = (int)insts.size();
     // the kernel's dynamic shared memory for these sizes (kernels_mega.cu, mega_smem_bytes)
     auto zb = [](size_t b) { return 2 * mega_align(b); };
     auto xb = [](int n, size_t b) { return (size_t)(kMegaThreads / mega_xy_threads(n)) * mega_align(b); };
