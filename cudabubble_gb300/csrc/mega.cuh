@@ -214,7 +214,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
             }
         }
         __syncthreads();
-        if (tid == 0) {
+        // the completion count from warp 1, so that its fence (which waits for this unit's
+        // stores) runs beside rank 0's thread 0 preparing the next hand-over
+        if (tid == 32) {
             CB_FENCE();  // this CTA's writes before its completion count
             const unsigned prev = atomicAdd(a.done + slot, 1u);
             if (task.phase == MP_XYC && prev + 1 == a.need[slot]) {
