@@ -62,7 +62,8 @@ struct MegaSlot {
     MegaTask task;
 };
 struct MegaHeadLayout {
-    MegaSlot cur[2];   // this CTA's unit of the round (round parity), written by rank 0
+    MegaSlot slot[2];  // rank 0's hand-over slots (round parity)
+    MegaSlot cur;      // this CTA's unit of the round
     MegaTask next;     // rank 0: the next unit's descriptor, streamed in under the current unit
     int last;          // the prologue's last-block flag
     int pad;
@@ -128,11 +129,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
     const int rank = (int)cl.block_rank();
     const int tid = threadIdx.x;
     MegaHeadLayout* h = reinterpret_cast<MegaHeadLayout*>(smem_raw);
-    MegaHeadLayout* peer = rank == 0 ? cl.map_shared_rank(h, 1) : nullptr;
+    const MegaSlot* src = rank == 0 ? h->slot : cl.map_shared_rank(h->slot, 0);
     unsigned char* sm = smem_raw + kMegaHead;
     const int ncache = a.ninst < kMegaInstCache ? a.ninst : kMegaInstCache;
     for (int i = tid; i < ncache; i += kMegaThreads) h->insts[i] = a.insts[i];
-    cl.sync();  // both CTAs run before rank 0 first writes into rank 1's shared memory
     unsigned claimed = 0;  // rank 0, thread 0: the unit of the next round
     if (rank == 0 && tid == 0) {
         claimed = atomicAdd(a.ticket, 1u);
@@ -141,7 +141,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
     for (int round = 0;; ++round) {
         if (rank == 0 && tid == 0) {
             // the round's unit, its descriptor and its dependency, checked before the hand-over
-            MegaSlot s;
+            MegaSlot& s = h->slot[round & 1];
             s.t = claimed;
             if (claimed < (unsigned)a.ntasks) {
                 mega_copy_wait();
@@ -164,18 +164,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
                     CB_FENCE();  // the previous phase's writes before this unit's reads
                 }
             }
-            // into both CTAs' slot of this round's parity: rank 1 read the other slot in the
-            // last round, and reads this one after the barrier below
-            h->cur[round & 1] = s;
-            peer->cur[round & 1] = s;
         }
-        // the round's unit is in both CTAs' slots, its dependency met; both CTAs are done with
-        // the last round.  The barrier's release / acquire makes rank 0's write of rank 1's slot
-        // visible there and passes rank 0's acquisition of the previous phase's writes on.
+        // the round's unit is in rank 0's slot, its dependency met; both CTAs are done with
+        // the last round.  The barrier's release / acquire passes rank 0's acquisition of the
+        // previous phase's writes on to rank 1.
         cl.sync();
-        const unsigned t = h->cur[round & 1].t;
+        if (tid == 0) h->cur = src[round & 1];
+        __syncthreads();
+        const unsigned t = h->cur.t;
         if (t >= (unsigned)a.ntasks) break;
-        const MegaTask task = h->cur[round & 1].task;
+        const MegaTask task = h->cur.task;
         if (rank == 0 && tid == 0) {  // claim the next unit and stream its descriptor in
             claimed = atomicAdd(a.ticket, 1u);
             if (claimed < (unsigned)a.ntasks) mega_copy16(&h->next, a.tasks + claimed);
