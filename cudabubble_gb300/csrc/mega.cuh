@@ -64,28 +64,23 @@ struct MegaSlot {
 struct MegaHeadLayout {
     MegaSlot slot[2];  // rank 0's hand-over slots (round parity)
     MegaSlot cur;      // this CTA's unit of the round
-    MegaTask next[2];  // rank 0: the descriptors of the next units, streamed in (round parity)
+    MegaTask next;     // rank 0: the next unit's descriptor, streamed in under the current unit
     int last;          // the prologue's last-block flag
     int pad;
     ProState pro;      // the prologue's block state
     const InstT<float>* insts[kMegaInstCache];
 };
 static_assert(sizeof(MegaHeadLayout) <= kMegaHead, "the head fits");
-static_assert(offsetof(MegaHeadLayout, next) % 16 == 0, "cp.async targets aligned");
+static_assert(offsetof(MegaHeadLayout, next) % 16 == 0, "cp.async target aligned");
 
-// a 16-byte global -> shared copy that completes asynchronously; mega_copy_commit closes
-// this thread's group of copies (possibly empty), and mega_copy_wait waits for all of them
+// a 16-byte global -> shared copy that completes asynchronously (this thread waits for it
+// with mega_copy_wait)
 __device__ __forceinline__ void mega_copy16(void* dst, const void* src) {
 #if defined(__CUDA_ARCH__)
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n\tcp.async.commit_group;" ::"r"(d), "l"(src) : "memory");
 #else
     memcpy(dst, src, 16);
-#endif
-}
-__device__ __forceinline__ void mega_copy_commit() {
-#if defined(__CUDA_ARCH__)
-    asm volatile("cp.async.commit_group;" ::: "memory");
 #endif
 }
 __device__ __forceinline__ void mega_copy_wait() {
@@ -138,42 +133,33 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
     unsigned char* sm = smem_raw + kMegaHead;
     const int ncache = a.ninst < kMegaInstCache ? a.ninst : kMegaInstCache;
     for (int i = tid; i < ncache; i += kMegaThreads) h->insts[i] = a.insts[i];
-    // rank 0, thread 0: the unit of this round and its descriptor, whether its dependency
-    // was seen complete when the round before began, and the unit of the next round (its
-    // descriptor streaming into next[(round + 1) & 1])
-    unsigned u_cur = 0, u_nxt = 0;
-    MegaTask d_cur = {};
-    bool seen = false;
+    unsigned claimed = 0;  // rank 0, thread 0: the unit of the next round
     if (rank == 0 && tid == 0) {
-        u_cur = atomicAdd(a.ticket, 1u);
-        if (u_cur < (unsigned)a.ntasks) d_cur = a.tasks[u_cur];
-        u_nxt = atomicAdd(a.ticket, 1u);
-        if (u_nxt < (unsigned)a.ntasks) mega_copy16(&h->next[1], a.tasks + u_nxt);
-        mega_copy_commit();
+        claimed = atomicAdd(a.ticket, 1u);
+        if (claimed < (unsigned)a.ntasks) h->next = a.tasks[claimed];
     }
     for (int round = 0;; ++round) {
         if (rank == 0 && tid == 0) {
             // the round's unit, its descriptor and its dependency, checked before the hand-over
             MegaSlot& s = h->slot[round & 1];
-            s.t = u_cur;
-            if (u_cur < (unsigned)a.ntasks) {
-                s.task = d_cur;
-                if (d_cur.phase != MP_PRO) {
-                    if (!seen) {
-                        const int dep = d_cur.inst * MP_N + d_cur.phase - 1;
-                        const volatile unsigned* d = a.done + dep;
-                        const volatile unsigned* failed = a.err;
-                        const unsigned need = a.need[dep];
-                        int n = 0;
-                        // once any wait of the launch has run out, none waits: the attempt is
-                        // void and ends without a further bound's delay per unit
-                        while (*d < need && *failed == 0u) {
-                            if (++n > CB_MEGA_SPIN) {
-                                atomicAdd(a.err, 1u);
-                                break;
-                            }
-                            __nanosleep(64);
+            s.t = claimed;
+            if (claimed < (unsigned)a.ntasks) {
+                mega_copy_wait();
+                s.task = h->next;
+                if (s.task.phase != MP_PRO) {
+                    const int dep = s.task.inst * MP_N + s.task.phase - 1;
+                    const volatile unsigned* d = a.done + dep;
+                    const volatile unsigned* failed = a.err;
+                    const unsigned need = a.need[dep];
+                    int n = 0;
+                    // once any wait of the launch has run out, none waits: the attempt is void
+                    // and ends without a further bound's delay per unit
+                    while (*d < need && *failed == 0u) {
+                        if (++n > CB_MEGA_SPIN) {
+                            atomicAdd(a.err, 1u);
+                            break;
                         }
+                        __nanosleep(64);
                     }
                     CB_FENCE();  // the previous phase's writes before this unit's reads
                 }
@@ -188,24 +174,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kMegaThreads, 2) meg
         const unsigned t = h->cur.t;
         if (t >= (unsigned)a.ntasks) break;
         const MegaTask task = h->cur.task;
-        if (rank == 0 && tid == 0) {
-            // advance: the next round's unit and descriptor (landed under the last round), a
-            // first look at its dependency, and the claim of the unit after it, whose
-            // descriptor streams in under this round's work.  The two loads overlap.
-            const unsigned u_after = atomicAdd(a.ticket, 1u);
-            u_cur = u_nxt;
-            seen = false;
-            if (u_cur < (unsigned)a.ntasks) {
-                mega_copy_wait();  // the descriptor's group, issued a round ago
-                d_cur = h->next[(round + 1) & 1];
-                if (d_cur.phase != MP_PRO) {
-                    const int dep = d_cur.inst * MP_N + d_cur.phase - 1;
-                    seen = *(const volatile unsigned*)(a.done + dep) >= a.need[dep];
-                }
-            }
-            u_nxt = u_after;
-            if (u_nxt < (unsigned)a.ntasks) mega_copy16(&h->next[round & 1], a.tasks + u_nxt);
-            mega_copy_commit();
+        if (rank == 0 && tid == 0) {  // claim the next unit and stream its descriptor in
+            claimed = atomicAdd(a.ticket, 1u);
+            if (claimed < (unsigned)a.ntasks) mega_copy16(&h->next, a.tasks + claimed);
         }
         const int slot = task.inst * MP_N + task.phase;
         const InstT<float>& I = task.inst < ncache ? *h->insts[task.inst] : *a.insts[task.inst];
