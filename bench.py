@@ -479,17 +479,23 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    t0 = time.perf_counter()
-    st.set_phi(pin_in.numpy())
-    rr = st.run(args.steps)
-    out = st.get_phi(out=pin_out.numpy())
-    sc2 = st.scalars()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    # the median of three passes, each from phi0 (the first pass also pays one-time costs of
+    # the pinned pages)
+    walls = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        st.set_phi(pin_in.numpy())
+        rr = st.run(args.steps)
+        out = st.get_phi(out=pin_out.numpy())
+        sc2 = st.scalars()
+        walls.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(sorted(walls)[1], world)
     e2e_steps = sc2["steps"]
     e2e = {"value": job_throughput(N, e2e_steps, e2e_s, world), "unit": UNIT,
            "h2d_bytes_per_step": int(p0.nbytes / max(e2e_steps, 1)),
            "d2h_bytes_per_step": int((out.nbytes + 120) / max(e2e_steps, 1)),
-           "what": "cb_set_phi(pinned host phi0) + cb_run(K) + cb_get_phi(pinned host) + cb_scalars_get, wall clock"}
+           "what": "cb_set_phi(pinned host phi0) + cb_run(K) + cb_get_phi(pinned host) + cb_scalars_get, wall clock, "
+                   "median of 3 passes"}
     st.close()
 
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
