@@ -18,6 +18,10 @@
 // Both CTAs run the same sequence of units and meet the same cluster barriers inside the
 // cluster xy body.  The instance pointers sit in shared memory from the start.
 //
+// Completion: after a unit, warp 1 of each CTA counts it in its instance's phase counter
+// behind a release fence (beside rank 0's preparation of the next hand-over), and the CTA
+// that completes an instance's candidate phase runs the instance's decision.
+//
 // Waits: rank 0's thread 0 polls the previous phase's completion counter of the unit's
 // instance with a bounded number of polls, then acquires; the cluster barrier passes that
 // on to rank 1.  A wait that runs out counts in err and the unit runs anyway (its results
