@@ -58,30 +58,6 @@ def test_split_matches_single_cta(cblib, n, nz, prec):
     assert abs(a1["E"] - b1["E"]) <= (1e-11 if prec == 0 else 1e-5) * abs(a1["E"])
 
 
-@pytest.mark.parametrize("n", [96, 128])
-def test_single_cta_planes_match_the_cluster_pass(cblib, n):
-    """The FP32 fused plane pass on one 1024-thread CTA per plane (xy_split = single)
-    against the default two-CTA clusters, on 96^2 and 128^2 planes: the same transforms
-    and pointwise arithmetic with other thread shapes, so the trajectories agree to the
-    summation order of the sums."""
-    from cudabubble_gb300 import capi, shapes
-    nz = 32
-    eps = shapes.eps_rule(150, n)
-    phi0 = shapes.seeded_ellipsoid(n, nz, eps, 9)
-    res = {}
-    for split in (capi.XYP_AUTO, capi.XYP_SINGLE):
-        st = _stepper(capi, n, nz, "etd2", capi.CB_FP32, split, time_step=1e-6, fixed_time_step=0.0)
-        st.set_phi(phi0)
-        st.run(20)
-        res[split] = (st.scalars(), st.get_phi())
-        st.close()
-    (a, ap), (b, bp) = res[capi.XYP_AUTO], res[capi.XYP_SINGLE]
-    assert (a["steps"], a["rejects"]) == (b["steps"], b["rejects"])
-    for k in ("E", "V", "S"):
-        assert abs(a[k] - b[k]) <= 1e-7 * abs(a[k]), (k, a[k], b[k])
-    assert np.abs(ap - bp).max() <= 1e-5
-
-
 @pytest.mark.parametrize("method", ["euler", "etd4"])
 def test_split_other_methods(cblib, method):
     from cudabubble_gb300 import capi, shapes
