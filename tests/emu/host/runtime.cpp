@@ -2,6 +2,9 @@
 // cuda_runtime.h beside this file.  Host memory, streams that run their work at once,
 // graphs as recorded closures, kernels run by emu::launch with one OS thread per CUDA
 // thread of a cluster, reused for every cluster of the grid.
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -36,6 +39,42 @@ static double now_ms() {
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
+// EMU_GUARD set: device buffers and shared memory are placed at the end of their own
+// mapping, between two 64 MB inaccessible regions, so an access far outside every
+// allocation (beyond AddressSanitizer's redzones, into another live allocation) faults
+static const size_t kGuard = (size_t)64 << 20;
+static bool guarded() {
+    static const bool g = getenv("EMU_GUARD") != nullptr;
+    return g;
+}
+static std::map<void*, std::pair<void*, size_t>> g_maps;
+static std::mutex g_map_mu;
+void* emu_alloc(size_t n, size_t align) {
+    if (!guarded()) return malloc(n ? n : 1);
+    const size_t pg = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t na = ((n ? n : 1) + align - 1) / align * align;
+    const size_t body = (na + pg - 1) / pg * pg;
+    const size_t total = kGuard + body + kGuard;
+    char* base = (char*)mmap(nullptr, total, PROT_NONE, MAP_PRIVATE | MAP_ANONYMOUS | MAP_NORESERVE, -1, 0);
+    if (base == MAP_FAILED) abort();
+    if (mprotect(base + kGuard, body, PROT_READ | PROT_WRITE)) abort();
+    void* p = base + kGuard + body - na;
+    std::lock_guard<std::mutex> lk(g_map_mu);
+    g_maps[p] = {base, total};
+    return p;
+}
+void emu_free(void* p) {
+    if (!guarded()) {
+        free(p);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_map_mu);
+    auto it = g_maps.find(p);
+    if (it == g_maps.end()) return;
+    munmap(it->second.first, it->second.second);
+    g_maps.erase(it);
+}
+
 void launch(dim3 grid, int nt, size_t smem, int clus, const std::function<void()>& body) {
     g_bdim = dim3(nt);
     g_gdim = grid;
@@ -44,7 +83,7 @@ void launch(dim3 grid, int nt, size_t smem, int clus, const std::function<void()
     std::vector<Block> blocks(clus);
     for (int r = 0; r < clus; ++r) {
         blocks[r].ex = new double[nt];
-        blocks[r].smem = (unsigned char*)malloc(smem ? smem : 1);
+        blocks[r].smem = (unsigned char*)emu_alloc(smem, 16);
         blocks[r].smem_bytes = smem;
         blocks[r].rank = r;
         blocks[r].cl = &cl;
@@ -88,7 +127,7 @@ void launch(dim3 grid, int nt, size_t smem, int clus, const std::function<void()
         });
     for (auto& x : th) x.join();
     for (auto& b : blocks) {
-        free(b.smem);
+        emu_free(b.smem);
         delete[] b.ex;
     }
 }
@@ -141,12 +180,12 @@ cudaError_t cudaGetLastError() {
 }
 const char* cudaGetErrorString(cudaError_t e) { return e ? "emulated error" : "no error"; }
 cudaError_t cudaMalloc(void** p, size_t n) {
-    *p = malloc(n ? n : 1);
+    *p = emu::emu_alloc(n, 256);
     memset(*p, 0xEE, n);
     return cudaSuccess;
 }
 cudaError_t cudaFree(void* p) {
-    free(p);
+    emu::emu_free(p);
     return cudaSuccess;
 }
 static void check_capture(cudaStream_t s, const char* what) {
