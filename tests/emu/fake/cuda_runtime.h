@@ -22,7 +22,10 @@
 #define __launch_bounds__(...)
 #define __cluster_dims__(...)
 #define __align__(n) alignas(n)
-#define __shared__
+// a kernel's static shared variable: one object for the whole launch, which is one block's
+// as the emulation runs the blocks of a one-CTA-cluster launch one at a time (no kernel
+// with a cluster of two declares one)
+#define __shared__ static
 
 struct float2 { float x, y; };
 struct alignas(16) float4 { float x, y, z, w; };

@@ -225,6 +225,12 @@ cudaError_t cudaEventCreate(cudaEvent_t* e) {
     *e = new emu::Event;
     return cudaSuccess;
 }
+cudaError_t cudaEventCreateWithFlags(cudaEvent_t* e, unsigned) { return cudaEventCreate(e); }
+// streams run their work at once, so every wait is already satisfied
+cudaError_t cudaStreamWaitEvent(cudaStream_t s, cudaEvent_t, unsigned) {
+    check_capture(s, "event wait");
+    return cudaSuccess;
+}
 cudaError_t cudaEventRecord(cudaEvent_t e, cudaStream_t s) {
     check_capture(s, "event record");
     e->t = emu::now_ms();
