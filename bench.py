@@ -49,6 +49,11 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# 32 hardware work queues for the process's streams (read when the CUDA context is made):
+# with the default 8, the served and batched workloads' per-class streams share queues
+# with each other and with the streams earlier workloads made, and a small class's
+# launches wait behind a large class's in the same queue
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 N_GRID = 128
 EPSSIZE = 150
