@@ -596,20 +596,32 @@ template <class T> struct Server {
         memset(&dummy, 0, sizeof dummy);
         dummy.ctrl = dummy_ctrl;
         long long maxN = 0;
+        std::vector<Eff> effs(n);
         for (int i = 0; i < n; ++i) {
-            Eff e;
-            int rc = make_params(reqs[i].params, e);
+            int rc = make_params(reqs[i].params, effs[i]);
             if (rc) return rc;
+        }
+        auto same_class = [](const Eff& a, const Eff& b) {
+            return a.p.nx == b.p.nx && a.p.nz == b.p.nz && a.p.method == b.p.method && a.accurate == b.accurate &&
+                   a.p.split == b.p.split && a.p.curv == b.p.curv;
+        };
+        for (int i = 0; i < n; ++i) {
+            const Eff& e = effs[i];
             if (!Launch<T>::xy_supported(e.p.nx) || !Launch<T>::z_supported(e.p.nz))
                 return fail(CB_EUNSUPPORTED, "request %d: grid %d^2x%d not built", i, e.p.nx, e.p.nz);
             maxN = std::max<long long>(maxN, e.p.N);
             if (find(e) >= 0) continue;
+            // the trace's requests of this class: no more slots than that, since every
+            // launch of the class graph runs (empty) CTAs for its free slots too
+            int members = 0;
+            for (int j = i; j < n; ++j) members += same_class(e, effs[j]) ? 1 : 0;
             ServeClass<T> c;
             c.nx = e.p.nx; c.nz = e.p.nz; c.method = e.p.method; c.accurate = e.accurate; c.split = e.p.split;
             c.curv = e.p.curv;
             c.bytes = (long long)instance_arena_bytes<T>(e.p);
             if (c.bytes > budget) return fail(CB_ENOMEM, "request %d needs %lld bytes, over the budget", i, c.bytes);
-            c.cap = (int)std::max<long long>(1, std::min<long long>(max_slots, budget / c.bytes));
+            c.cap = (int)std::max<long long>(1, std::min<long long>({(long long)max_slots, budget / c.bytes,
+                                                                     (long long)members}));
             const int tx = Launch<T>::z_tile();
             c.ntiles = (e.p.ny * e.p.nc + tx - 1) / tx;
             // attempts per launch batch: more for small grids, whose attempts are short
