@@ -53,8 +53,10 @@ struct YArgs {
 enum SpecMul { SM_NONE = 0, SM_LAP = 1, SM_DX = 2, SM_DY = 3, SM_DZ = 4 };
 
 // state_io bits for the plain z modes: the spectrum read (1) or written (2) is
-// a stepped state field (double-float pairs in the FP32 form)
-enum { IO_CIN_STATE = 1, IO_COUT_STATE = 2 };
+// a stepped state field (double-float pairs in the FP32 form); in the FP64 pass,
+// the spectrum read (4) or written (8) is the FP32 form's state, as double-float
+// pairs (hi.x, hi.y, lo.x, lo.y) with hi = fl32(v), lo = fl32(v - hi)
+enum { IO_CIN_STATE = 1, IO_COUT_STATE = 2, IO_CIN_FF = 4, IO_COUT_FF = 8 };
 
 struct ZArgs {
     int mode;

@@ -29,8 +29,6 @@ template <class T> struct Launch {
     // the full ETD N-hat of instance 0 (its Nu buffer, plus the FP32 form's linear part on `spec`)
     static cudaError_t nhat_full(const InstT<T>* d, const void* spec, double* out, size_t n, cudaStream_t s);
     static cudaError_t state_to_double(const void* in, double* out, size_t n, cudaStream_t s);
-    // complex double spectrum <-> stepped state of precision T (to_state = 1: double -> state)
-    static cudaError_t f64_to_state(const void* in, void* out, size_t n, int to_state, cudaStream_t s);
 };
 
 cudaError_t launch_pointwise(int kind, size_t n, double* out, const double* a, const double* b, const double* c,

@@ -361,13 +361,6 @@ template <class T> cudaError_t Launch<T>::state_to_double(const void* in, double
     return cudaGetLastError();
 }
 
-template <class T>
-cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_state, cudaStream_t s) {
-    const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    f64_state_kernel<T><<<blocks, 256, 0, s>>>(in, out, n, to_state);
-    return cudaGetLastError();
-}
-
 }  // namespace cb
 
 // explicit instantiation, split in two translation units per precision so the
@@ -385,8 +378,7 @@ cudaError_t Launch<T>::f64_to_state(const void* in, void* out, size_t n, int to_
     template cudaError_t cb::Launch<T>::coef(const cb::InstT<T>*, int, int, cudaStream_t, int);                    \
     template cudaError_t cb::Launch<T>::to_double(const void*, double*, size_t, cudaStream_t);                     \
     template cudaError_t cb::Launch<T>::nhat_full(const cb::InstT<T>*, const void*, double*, size_t, cudaStream_t); \
-    template cudaError_t cb::Launch<T>::state_to_double(const void*, double*, size_t, cudaStream_t);               \
-    template cudaError_t cb::Launch<T>::f64_to_state(const void*, void*, size_t, int, cudaStream_t);
+    template cudaError_t cb::Launch<T>::state_to_double(const void*, double*, size_t, cudaStream_t);
 #define CB_INSTANTIATE_Z(T)                                    \
     template bool cb::Launch<T>::z_supported(int);             \
     template int cb::Launch<T>::z_tile();                      \

@@ -401,27 +401,6 @@ __global__ void state_to_double_kernel(const void* __restrict__ in, double2* __r
     }
 }
 
-// complex double spectrum <-> stepped state: FP64 copy, or the double-float
-// split hi = fl32(v), lo = fl32(v - hi) of the FP32 form
-template <class T>
-__global__ void f64_state_kernel(const void* __restrict__ in, void* __restrict__ out, size_t n, int to_state) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (sizeof(T) == 4) {
-            if (to_state) {
-                const double2 v = reinterpret_cast<const double2*>(in)[i];
-                const float hx = __double2float_rn(v.x), hy = __double2float_rn(v.y);
-                reinterpret_cast<float4*>(out)[i] =
-                    make_float4(hx, hy, __double2float_rn(v.x - (double)hx), __double2float_rn(v.y - (double)hy));
-            } else {
-                const float4 q = reinterpret_cast<const float4*>(in)[i];
-                reinterpret_cast<double2*>(out)[i] = make_double2((double)q.x + (double)q.z, (double)q.y + (double)q.w);
-            }
-        } else {
-            reinterpret_cast<double2*>(out)[i] = reinterpret_cast<const double2*>(in)[i];
-        }
-    }
-}
-
 // full N-hat = N'-hat + c_lin u-hat of the FP32 form's split (lin_coef), in FP64,
 // for the field getter; the FP64 form keeps the full N-hat in Nu
 template <class T>

@@ -539,9 +539,8 @@ template <class T> class Stepper final : public Handle {
         CB_CK(push());
         // FP32 form: the state's real-space field, exact as a double-float pair
         if (sizeof(T) == 4) CB_CK(launch_real_to_ff(src, h.U[0], (size_t)p.nz * p.ny, p.nx, st));
-        if (aux) {  // exact spectrum: FP64 transform into the 16 B/mode candidate field, then hi/lo split
-            CB_CK(fwd3d_f64(src, h.spec[1], h.ahat));
-            CB_CK(Launch<T>::f64_to_state(h.spec[1], h.spec[0], ns, 1, st));
+        if (aux) {  // exact spectrum: FP64 transform, split hi/lo into the state by its z pass
+            CB_CK(fwd3d_f64(src, h.spec[0], h.ahat));
         } else {
             CB_CK(fwd3d(src, h.spec[0], h.A, true));
         }
@@ -575,10 +574,8 @@ template <class T> class Stepper final : public Handle {
         if (!have_state) return fail(CB_EINVAL, "no state: call cb_set_phi first");
         CB_CK(pull());
         double* dst = dev ? out : stage();
-        if (aux) {
-            void* s64 = h.spec[1 - hc.spec_state];  // candidate slot: free between attempts
-            CB_CK(Launch<T>::f64_to_state(h.spec[hc.spec_state], s64, ns, 0, st));
-            CB_CK(inv3d_f64(s64, dst, h.ahat));
+        if (aux) {  // FP64 transform of the state, joined from its hi/lo pairs by its z pass
+            CB_CK(inv3d_f64(h.spec[hc.spec_state], dst, h.ahat));
         } else {
             CB_CK(inv3d(h.spec[hc.spec_state], SM_NONE, dst, h.A, true));
         }
@@ -1161,8 +1158,9 @@ template <class T> class Stepper final : public Handle {
         z.cout = spec;
         return Launch<T>::z(p.nz, d, 1, ntiles, z, st);
     }
-    // FP64 plain transforms over the auxiliary descriptor (FP32 form only)
-    cudaError_t fwd3d_f64(const double* src, void* spec64, void* part64) {
+    // FP64 plain transforms over the auxiliary descriptor (FP32 form only), between the
+    // real double field and the FP32 form's double-float state spectrum
+    cudaError_t fwd3d_f64(const double* src, void* state, void* part64) {
         XYArgs a;
         memset(&a, 0, sizeof a);
         a.mode = XY_FWD_PLAIN;
@@ -1173,15 +1171,17 @@ template <class T> class Stepper final : public Handle {
         ZArgs z;
         memset(&z, 0, sizeof z);
         z.mode = Z_FWD_PLAIN;
+        z.state_io = IO_COUT_FF;
         z.cin = part64;
-        z.cout = spec64;
+        z.cout = state;
         return Launch<double>::z(p.nz, aux, 1, ntiles64(), z, st);
     }
-    cudaError_t inv3d_f64(const void* spec64, double* dst, void* part64) {
+    cudaError_t inv3d_f64(const void* state, double* dst, void* part64) {
         ZArgs z;
         memset(&z, 0, sizeof z);
         z.mode = Z_INV_PLAIN;
-        z.cin = spec64;
+        z.state_io = IO_CIN_FF;
+        z.cin = state;
         z.cout = part64;
         cudaError_t r = Launch<double>::z(p.nz, aux, 1, ntiles64(), z, st);
         if (r != cudaSuccess) return r;

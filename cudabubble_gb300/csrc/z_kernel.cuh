@@ -264,6 +264,14 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
             const int kz = tidx<NZ>(r);
             const C v = S[r * W + c];
             const C o = cmk<C>(k.k_invN.mul(v.x), k.k_invN.mul(v.y));
+            if constexpr (sizeof(T) == 8) {
+                if (a.state_io & IO_COUT_FF) {  // the FP32 form's state, split in this pass
+                    const float hx = __double2float_rn(o.x), hy = __double2float_rn(o.y);
+                    reinterpret_cast<float4*>(a.cout)[(size_t)kz * Mc + m] =
+                        make_float4(hx, hy, __double2float_rn(o.x - (double)hx), __double2float_rn(o.y - (double)hy));
+                    continue;
+                }
+            }
             if (to_state) State<T>::from(o).store(a.cout, (size_t)kz * Mc + m);
             else out[(size_t)kz * Mc + m] = o;
         }
@@ -513,8 +521,14 @@ __device__ __forceinline__ void z_body(const InstT<T>& I, const int tile, const 
             default: {  // Z_INV_PLAIN with an optional spectral multiplier
                 if constexpr (!gp) break;
                 have_state = false;
-                const C v = (a.state_io & IO_CIN_STATE) ? State<T>::load(a.cin, g).work()
-                                                        : reinterpret_cast<const C*>(a.cin)[g];
+                C v;
+                if (sizeof(T) == 8 && (a.state_io & IO_CIN_FF)) {  // the FP32 form's state, joined here
+                    const float4 q = __ldg(reinterpret_cast<const float4*>(a.cin) + g);
+                    v = cmk<C>((T)((double)q.x + (double)q.z), (T)((double)q.y + (double)q.w));
+                } else {
+                    v = (a.state_io & IO_CIN_STATE) ? State<T>::load(a.cin, g).work()
+                                                    : reinterpret_cast<const C*>(a.cin)[g];
+                }
                 if (a.mul == SM_LAP) {
                     const int kk = kx * kx + kyf * kyf + kzf * kzf;
                     if constexpr (sizeof(T) == 8) {
